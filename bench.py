@@ -1,0 +1,389 @@
+#!/usr/bin/env python
+"""Throughput of the Lomb-Scargle hot path on one GB300, one JSON line on stdout.
+
+Workload (the reference's headline batch): 999 objects with log-normal observation
+counts (round(LogNormal(ln 150, 0.6)) clipped to [20, 1500], ~150k rows, seeded,
+synthetic), standard L-S, 1e6 angular frequencies in [1.005, 150.796). One step =
+one batch periodogram with the fused per-object argmax, mixed precision form, inputs
+resident in HBM. Metric: observation x frequency pairs per second.
+
+Also reported on the same line:
+  plain_fp64   the FP64 drop-in form on the first frequencies of the same grid;
+  e2e          the engine's host-buffer C ABI (lsgb_periodogram_host): pinned host
+               inputs in, best index/power out, copies inside the timed region;
+  e2e_dropin   LombScarglePy of libpylsnoerrorfloat.so (MODE 1) returning the full
+               periodogram to a host buffer, as source/lombscarglegpu.py calls it;
+  roofline     the mixed kernel's FP32-pipe ops (8 per pair) per second against the
+               FP32 FMA peak measured in the same run (cuBLAS SGEMM, TF32 off);
+  cpu_baseline the FP64 oracle (the reference's CPU algorithm) on all host cores;
+  clocks       nvidia-smi samples taken during the timed region.
+`--impl reference` runs the reference arm: the reference's CPU algorithm on the
+host cores (its own build when it is present, else the oracle port).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "obs x freq pairs/s (mixed FP32-recurrence form, 1 GB300)"
+UNIT = "pairs/s"
+OPS_PER_PAIR_STD = 8  # 4 rotation + 4 accumulation FP32-pipe ops per (obs, freq) pair
+L2_FLUSH_BYTES = 256 << 20
+
+
+def rank_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(
+        os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+        return False
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def fp32_peak_ops(torch, dev):
+    """FP32 FMA throughput of cuBLAS SGEMM (TF32 off), in FMA ops/s, best of 5."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        n = 8192
+        a = torch.randn(n, n, device=dev)
+        b = torch.randn(n, n, device=dev)
+        for _ in range(2):
+            torch.mm(a, b)
+        best = 1e30
+        for _ in range(5):
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            torch.mm(a, b)
+            e.record()
+            e.synchronize()
+            best = min(best, s.elapsed_time(e) / 1e3)
+        return n ** 3 / best
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+
+
+def cpu_baseline(w, n_freq_sample: int):
+    """The FP64 oracle (reference CPU algorithm) on the first n_freq_sample frequencies."""
+    from oracle import pyoracle
+
+    ws = w.subset_freqs(n_freq_sample)
+    t0 = time.perf_counter()
+    pyoracle.batch_pgram(0, ws.t, ws.y, None, ws.offsets, ws.fmin, ws.df, n_freq=ws.n_freq)
+    dt = time.perf_counter() - t0
+    return {"value": ws.pairs / dt, "unit": UNIT, "cores": pyoracle.max_threads(), "kind": "port",
+            "sample": f"{w.n_obj} objects x first {n_freq_sample} of {w.n_freq} frequencies "
+                      f"({ws.pairs:.3g} pairs, {dt:.2f} s)"}
+
+
+def reference_arm(args):
+    """The reference's CPU path on this host (all cores), bounded sample per step."""
+    from gpu_lomb_scargle_gb300 import synth
+
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return
+    w = synth.lognormal_batch()
+    nf = args.ref_freqs
+    ws = w.subset_freqs(nf)
+    kind, cores = "port", None
+    ref_lib = ROOT / "oracle" / "_ref" / "libpylsnoerrordouble.so"
+    run = None
+    try:
+        import ctypes
+        lib = ctypes.CDLL(str(ref_lib))
+        arr = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+        uarr = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
+        lib.LombScarglePy.argtypes = [uarr, arr, arr, arr, ctypes.c_uint, ctypes.c_double,
+                                      ctypes.c_double, ctypes.c_uint, ctypes.c_int, arr]
+        pg = np.zeros(ws.n_obj * nf)
+        ids = np.ascontiguousarray(ws.obj_id, np.uint32)
+        dy = np.ones(ws.n_rows)
+        import tempfile
+        tmp = tempfile.mkdtemp()
+
+        def run():
+            cwd = os.getcwd()
+            os.chdir(tmp)
+            try:
+                lib.LombScarglePy(ids, ws.t, ws.y.copy(), dy, ws.n_rows, ws.fmin, ws.fmax, nf, 4, pg)
+            finally:
+                os.chdir(cwd)
+        kind, cores = "reference", os.cpu_count()
+    except OSError:
+        from oracle import pyoracle
+
+        def run():
+            pyoracle.batch_pgram(0, ws.t, ws.y, None, ws.offsets, ws.fmin, ws.df, n_freq=nf)
+        cores = pyoracle.max_threads()
+    devnull = os.open(os.devnull, os.O_WRONLY)
+    saved = os.dup(1)
+    os.dup2(devnull, 1)  # the reference library prints progress to stdout
+    try:
+        for _ in range(args.warmup):
+            run()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            run()
+        dt = (time.perf_counter() - t0) / args.steps
+    finally:
+        sys.stdout.flush()
+        os.dup2(saved, 1)
+        os.close(saved)
+        os.close(devnull)
+    value = ws.pairs / dt
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded log-normal batch, stands in for the reference's missing "
+                    "999-object file)",
+            "config": {"workload": "lognormal_999obj_1e6freq_standard", "n_obj": w.n_obj,
+                       "rows": w.n_rows, "n_freq": w.n_freq, "sample_freqs": nf},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                             "sample": f"{w.n_obj} objects x first {nf} of {w.n_freq} frequencies "
+                                       f"per step ({ws.pairs:.3g} pairs)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="lsgb", choices=["lsgb", "reference"])
+    ap.add_argument("--n-freq", type=int, default=1_000_000)
+    ap.add_argument("--plain-freqs", type=int, default=20_000,
+                    help="frequencies of the plain FP64 comparison (0 = skip)")
+    ap.add_argument("--cpu-freqs", type=int, default=10_000,
+                    help="frequencies of the CPU-baseline sample (0 = skip)")
+    ap.add_argument("--ref-freqs", type=int, default=2_000,
+                    help="frequencies per step of the reference arm")
+    ap.add_argument("--no-dropin", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    import torch
+
+    from gpu_lomb_scargle_gb300 import engine as E
+    from gpu_lomb_scargle_gb300 import synth
+
+    rank, world, local = rank_info()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    # weak scaling: every rank owns its own batch of the same shape
+    w = synth.lognormal_batch(seed=2000 + rank, n_freq=args.n_freq)
+    eng = E.Engine(local)
+    t = torch.from_numpy(w.t).to(dev)
+    y = torch.from_numpy(w.y).to(dev)
+    bi = torch.empty(w.n_obj, dtype=torch.int32, device=dev)
+    bp = torch.empty(w.n_obj, dtype=torch.float64, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        eng.run_device(0, "mixed", t, y, None, w.offsets, w.fmin, w.df, w.n_freq, True, None, bi,
+                       bp, stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    kern_ms = []
+    launches = 0
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            flush.zero_()  # L2 flush between timed steps (outside the events)
+            starts[i].record(stream)
+            step()
+            ends[i].record(stream)
+            kern_ms.append(eng.last_kernel_ms())
+            launches += eng.launch_info()[0]
+        torch.cuda.synchronize()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    ms = float(np.mean(step_ms))
+    if world > 1:
+        tt = torch.tensor([ms], dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms = float(tt.item())
+    value = w.pairs * world / (ms / 1e3)
+    best_idx = bi.cpu().numpy()
+
+    if rank != 0:
+        return
+    clocks = clk.summary()
+    kms = float(np.mean(kern_ms))
+    ops = w.pairs * OPS_PER_PAIR_STD
+    peak_ops = fp32_peak_ops(torch, dev)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    achieved = ops / (kms / 1e3)
+    roofline = {"bound": "fp32", "achieved": achieved / 1e12, "peak": peak_ops / 1e12,
+                "unit": "Tops/s (FP32 pipe ops)", "frac": achieved / peak_ops, "traffic": None,
+                "peak_source": "cuBLAS SGEMM 8192^3, TF32 off, measured in this run (FMA ops/s)",
+                "ops_per_pair": OPS_PER_PAIR_STD, "kernel_ms": kms,
+                "frac_of_nominal_at_sampled_clock": (
+                    achieved / (128 * sms * clocks["sm_mhz"] * 1e6) if clocks["sm_mhz"] else None)}
+
+    extra = {}
+    # plain FP64 drop-in form on the first plain_freqs frequencies
+    if args.plain_freqs:
+        wp = w.subset_freqs(args.plain_freqs)
+        eng.run_device(0, "plain", t, y, None, wp.offsets, wp.fmin, wp.df, wp.n_freq, True, None,
+                       bi, bp, stream)
+        torch.cuda.synchronize()
+        pm = []
+        for _ in range(2):
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            flush.zero_()
+            s.record(stream)
+            eng.run_device(0, "plain", t, y, None, wp.offsets, wp.fmin, wp.df, wp.n_freq, True,
+                           None, bi, bp, stream)
+            e.record(stream)
+            e.synchronize()
+            pm.append(s.elapsed_time(e))
+        pv = wp.pairs / (np.mean(pm) / 1e3)
+        extra["plain_fp64"] = {"value": pv, "unit": UNIT, "ms_per_step": float(np.mean(pm)),
+                               "sample": f"first {args.plain_freqs} frequencies of the same grid"}
+        extra["mixed_over_plain"] = value / pv
+
+    # e2e through the host-buffer C ABI with pinned inputs
+    th = torch.from_numpy(w.t).pin_memory().numpy()
+    yh = torch.from_numpy(w.y).pin_memory().numpy()
+    oi = torch.empty(w.n_obj, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+    op = torch.empty(w.n_obj, dtype=torch.float64).pin_memory().numpy()
+    for _ in range(2):
+        eng.run_host(0, "mixed", th, yh, None, w.offsets, w.fmin, w.df, w.n_freq, True,
+                     out_idx=oi, out_power=op)
+    e2e_t = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        eng.run_host(0, "mixed", th, yh, None, w.offsets, w.fmin, w.df, w.n_freq, True,
+                     out_idx=oi, out_power=op)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e = {"value": w.pairs / float(np.mean(e2e_t)), "unit": UNIT,
+           "h2d_bytes_per_step": int(th.nbytes + yh.nbytes + 8 * (w.n_obj + 1)),
+           "d2h_bytes_per_step": int(oi.nbytes + op.nbytes),
+           "api": "lsgb_periodogram_host (C ABI), pinned host buffers, best period per object"}
+    if not np.array_equal(oi, best_idx.astype(np.uint32)):
+        e2e["mismatch_vs_device_path"] = True
+
+    if not args.no_dropin:
+        from gpu_lomb_scargle_gb300 import lombscarglegpu as lsg
+        lib = lsg._library(False, "float")
+        t32 = np.ascontiguousarray(w.t, np.float32)
+        y32 = np.ascontiguousarray(w.y, np.float32)
+        ids = np.ascontiguousarray(w.obj_id, np.uint32)
+        ones = np.ones(w.n_rows, np.float32)
+        pg = np.zeros(w.n_obj * w.n_freq, np.float32)
+        dt = []
+        devnull = os.open(os.devnull, os.O_WRONLY)
+        saved = os.dup(1)
+        sys.stdout.flush()
+        os.dup2(devnull, 1)
+        try:
+            for i in range(3):
+                t0 = time.perf_counter()
+                lib.LombScarglePy(ids, t32, y32, ones, w.n_rows, w.fmin, w.fmax, w.n_freq, 1, pg)
+                if i:
+                    dt.append(time.perf_counter() - t0)
+        finally:
+            sys.stdout.flush()
+            os.dup2(saved, 1)
+            os.close(saved)
+            os.close(devnull)
+        extra["e2e_dropin"] = {"value": w.pairs / float(np.mean(dt)), "unit": UNIT,
+                               "h2d_bytes_per_step": int(t32.nbytes * 3 + ids.nbytes),
+                               "d2h_bytes_per_step": int(pg.nbytes),
+                               "api": "LombScarglePy, libpylsnoerrorfloat.so, MODE 1, full pgram"}
+        del pg
+
+    cpu = cpu_baseline(w, args.cpu_freqs) if args.cpu_freqs else None
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (FP64 phase anchors)",
+            "data": "synthetic (seeded log-normal batch, stands in for the reference's missing "
+                    "999-object file)",
+            "config": {"workload": "lognormal_999obj_1e6freq_standard", "n_obj": w.n_obj,
+                       "rows": w.n_rows, "n_freq": w.n_freq, "form": "mixed", "seed": w.seed,
+                       "l2": "flushed between timed steps (256 MiB write)",
+                       "fmin": w.fmin, "fmax": w.fmax},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "gpu_launches": launches, **extra}
+    print(json.dumps(line), flush=True)
+    eng.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,70 @@
+"""Loading of the in-tree native libraries (built by ``gpu_lomb_scargle_gb300.build``).
+
+There is no Python or CPU fallback: if a library is missing, loading raises
+``NativeLibraryMissing`` with the build command to run.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+LIB_DIR = Path(__file__).resolve().parent / "lib"
+
+DROPIN_LIBS = ("libpylsnoerrorfloat.so", "libpylsnoerrordouble.so", "libpylserrorfloat.so",
+               "libpylserrordouble.so")
+
+# Symbols each library must export (the declarations of include/lsgb.h and
+# include/lombscargle_py.h).
+LSGB_SYMBOLS = ("lsgb_engine_create", "lsgb_engine_destroy", "lsgb_last_error", "lsgb_version",
+                "lsgb_periodogram_device", "lsgb_periodogram_host", "lsgb_set_tuning",
+                "lsgb_last_launch_info", "lsgb_last_kernel_time")
+PYABI_SYMBOLS = ("LombScarglePy", "LombScarglePy_last_status")
+
+
+class NativeLibraryMissing(RuntimeError):
+    pass
+
+
+_cache: dict[str, ctypes.CDLL] = {}
+
+
+def lib_path(name: str) -> Path:
+    return LIB_DIR / name
+
+
+def load(name: str) -> ctypes.CDLL:
+    if name in _cache:
+        return _cache[name]
+    p = lib_path(name)
+    if not p.exists():
+        raise NativeLibraryMissing(
+            f"{p} is not built; run `python -m gpu_lomb_scargle_gb300.build` (CUDA 13, sm_103a)")
+    lib = ctypes.CDLL(str(p))
+    _cache[name] = lib
+    return lib
+
+
+def lsgb() -> ctypes.CDLL:
+    lib = load("liblsgb.so")
+    if not getattr(lib, "_lsgb_typed", False):
+        c = ctypes
+        vp, u32, u64p, dbl, i32 = c.c_void_p, c.c_uint32, c.POINTER(c.c_uint64), c.c_double, c.c_int
+        lib.lsgb_engine_create.argtypes = [i32, c.POINTER(vp)]
+        lib.lsgb_engine_create.restype = i32
+        lib.lsgb_engine_destroy.argtypes = [vp]
+        lib.lsgb_engine_destroy.restype = None
+        lib.lsgb_last_error.restype = c.c_char_p
+        lib.lsgb_version.restype = c.c_char_p
+        common = [vp, i32, i32, i32, vp, vp, vp, u64p, u32, dbl, dbl, u32, i32, vp, vp, vp]
+        lib.lsgb_periodogram_device.argtypes = common + [vp]
+        lib.lsgb_periodogram_device.restype = i32
+        lib.lsgb_periodogram_host.argtypes = common
+        lib.lsgb_periodogram_host.restype = i32
+        lib.lsgb_set_tuning.argtypes = [vp, i32, i32, i32]
+        lib.lsgb_set_tuning.restype = i32
+        lib.lsgb_last_launch_info.argtypes = [vp, c.POINTER(c.c_uint32), c.POINTER(c.c_uint64)]
+        lib.lsgb_last_launch_info.restype = i32
+        lib.lsgb_last_kernel_time.argtypes = [vp, c.POINTER(c.c_float)]
+        lib.lsgb_last_kernel_time.restype = i32
+        lib._lsgb_typed = True
+    return lib

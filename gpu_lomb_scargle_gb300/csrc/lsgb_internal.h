@@ -1,0 +1,94 @@
+// lsgb_internal.h -- types shared by the kernels (lsgb_kernels.cu) and the host
+// engine (lsgb_engine.cu). Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace lsgb {
+
+// One observation as the mixed kernel consumes it (32 bytes, two 16-byte halves).
+//   a = frac(f0 * t)  and  b = frac(dfturn * t)  in units of 2^-64 turns, where
+//   f0 = fmin / 2pi and dfturn = df / 2pi, so the phase of grid point k is
+//   a + k*b (mod 2^64), exact to ~(1+k) * 2^-64 turns;
+//   cd, sd = cos, sin(2 pi b): the per-step rotation of the recurrence;
+//   standard:    v0 = y,          v1 = 0
+//   generalized: v0 = w / W,      v1 = (w / W) * (y - ybar_w),   w = 1/dy^2.
+struct __align__(16) ObsRec {
+    uint32_t a_lo, a_hi, b_lo, b_hi;
+    float v0, v1, cd, sd;
+};
+static_assert(sizeof(ObsRec) == 32, "ObsRec must be 32 bytes");
+
+// Per-object parameters, indexed by the caller's object index.
+struct ObjInfo {
+    uint64_t row0;  // first row of the object in t / y / dy / records
+    uint32_t n;     // rows
+    uint32_t pad;
+    double norm;    // standard: 2/(N var(y)) or 1; generalized mixed: 1 / weighted var(y)
+    double wtot;    // generalized: sum of 1/dy^2
+    double ymean;   // generalized: sum(y/dy^2) / sum(1/dy^2)
+    double wsum_f;  // generalized mixed: sum of the stored float weights (~1)
+    double ybar_f;  // generalized mixed: sum of the stored float w*y' / wsum_f (~0)
+};
+
+// Best (power, index) of one (object, frequency tile).
+struct TileBest {
+    double p;
+    uint32_t k;
+    uint32_t pad;
+};
+
+// Frequency grid in turns per unit time as double-double values.
+struct GridTurns {
+    double f0_hi, f0_lo;  // fmin / 2pi
+    double df_hi, df_lo;  // df / 2pi
+};
+
+struct MixedArgs {
+    const ObsRec *rec;
+    const ObjInfo *objs;
+    const uint32_t *perm;  // work order: objects by decreasing size
+    uint32_t n_obj, n_tiles, n_freq, chunk;
+    uint32_t *counter;     // persistent work-queue head (zeroed before launch)
+    void *pgram;           // [n_obj x n_freq] or null
+    TileBest *tile_best;   // [n_obj x n_tiles] or null
+};
+
+struct PlainArgs {
+    const void *t, *y, *dy;
+    const ObjInfo *objs;
+    const uint32_t *perm;
+    uint32_t n_obj, n_tiles, n_freq, chunk;
+    double fmin, df;
+    uint32_t *counter;
+    void *pgram;
+    TileBest *tile_best;
+};
+
+// Compiled tile shapes of the mixed kernel (frequencies per thread x threads).
+struct MixedShape {
+    int f, nt;
+};
+
+// ---- launchers (lsgb_kernels.cu); all asynchronous on `st` ----
+cudaError_t launch_stats(int variant, int mixed, int dtype, int normalize, const void *y,
+                         const void *dy, ObjInfo *objs, uint32_t n_obj, cudaStream_t st);
+cudaError_t launch_records(int variant, int dtype, const void *t, const void *y, const void *dy,
+                           const uint64_t *offsets, uint32_t n_obj, const ObjInfo *objs,
+                           uint64_t rows, GridTurns g, ObsRec *rec, cudaStream_t st);
+// Mixed kernel: returns cudaErrorInvalidValue when (variant, dtype, shape) is not compiled.
+cudaError_t launch_mixed(int variant, int dtype, MixedShape shape, const MixedArgs &a,
+                         int grid, size_t smem, cudaStream_t st);
+cudaError_t mixed_occupancy(int variant, int dtype, MixedShape shape, size_t smem, int *blocks);
+cudaError_t launch_plain(int variant, int in_dtype, int out_dtype, const PlainArgs &a, int grid,
+                         size_t smem, cudaStream_t st);
+cudaError_t plain_occupancy(int variant, int in_dtype, int out_dtype, size_t smem, int *blocks);
+cudaError_t launch_best_reduce(int dtype, const TileBest *tb, uint32_t n_obj, uint32_t n_tiles,
+                               uint32_t *best_idx, void *best_power, cudaStream_t st);
+
+constexpr int kPlainThreads = 256;
+constexpr uint32_t kMixedChunkMax = 2048;  // observations staged in shared memory per pass
+constexpr uint32_t kPlainChunkMax = 2048;
+
+}  // namespace lsgb

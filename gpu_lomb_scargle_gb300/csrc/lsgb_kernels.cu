@@ -1,0 +1,700 @@
+// lsgb_kernels.cu -- sm_103a kernels of the Lomb-Scargle engine.
+//
+// The hot path of the reference is the (object, frequency) double loop of
+// source/kernel.cu:484-631 (lombscargleBatch, standard L-S) and :368-477
+// (lombscargleBatchError, generalized L-S), plus their single-object forms
+// (:76-361). Here one persistent kernel per form walks a work queue of
+// (object, frequency tile) units, largest objects first, stages the object's
+// observations in shared memory, and fuses the power, the optional periodogram
+// store and the per-tile argmax into the same pass.
+//
+// Two precision forms:
+//  * plain FP64 (drop-in): sincos(omega_k * t_j) in FP64 for every pair and the
+//    reference's tau / power formulas in FP64 (with FP64 atan2; the reference's
+//    GPU double build silently uses FP32 atan2f, source/kernel.cu:228/:563, because
+//    `#if DTYPE==float` compares two undefined identifiers);
+//  * mixed: the phase of every (observation, frequency-run start) comes exactly
+//    from a 64-bit fixed-point anchor (a + k*b mod 2^64 turns), its sine/cosine from
+//    the SFU, and the next F-1 frequencies of the run by an FP32 angle-addition
+//    recurrence (rotation by the observation's per-step cos/sin). tau never needs an
+//    arctangent: the power is a closed rational function of the sums and
+//    r = hypot(CC-SS, 2CS) (the tau-rotated formula of source/main.cu:1588-1598
+//    expanded with the double-angle identities).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "lsgb_internal.h"
+
+namespace lsgb {
+
+namespace {
+
+constexpr double kTwoPi = 6.283185307179586;
+constexpr double kTwoPiOver2p64 = 3.4061215800865545e-19;  // 2 pi / 2^64
+constexpr float kTwoPiOver2p32f = 1.4629180792671596e-09f;  // 2 pi / 2^32
+constexpr double k2p64 = 18446744073709551616.0;
+
+template <typename T>
+__device__ __forceinline__ double ld_as_double(const void *p, uint64_t i) {
+    return (double)__ldg(reinterpret_cast<const T *>(p) + i);
+}
+
+__device__ __forceinline__ double load_in(int dtype, const void *p, uint64_t i) {
+    return dtype == 0 ? ld_as_double<float>(p, i) : ld_as_double<double>(p, i);
+}
+
+// Block-wide sum of doubles (blockDim.x a multiple of 32, <= 1024).
+__device__ double block_sum(double v, double *s_red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) s_red[w] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (w == 0) {
+        r = (l < (int)(blockDim.x >> 5)) ? s_red[l] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+        if (l == 0) s_red[0] = r;
+    }
+    __syncthreads();
+    r = s_red[0];
+    __syncthreads();
+    return r;
+}
+
+// frac(x * t) as a 64-bit fixed-point fraction of a turn, x = x_hi + x_lo
+// (double-double). Error below 2^-60 turns for |x t| < 2^40.
+__device__ __forceinline__ uint64_t frac_turns_u64(double x_hi, double x_lo, double t) {
+    const double p_hi = x_hi * t;
+    const double p_lo = fma(x_hi, t, -p_hi) + x_lo * t;
+    const double r_hi = p_hi - floor(p_hi);  // exact, in [0, 1)
+    const uint64_t u = __double2ull_rz(r_hi * k2p64);
+    const long long e = __double2ll_rn(p_lo * k2p64);
+    return u + (uint64_t)e;
+}
+
+// (power, index) ordering of the reference's argmax (source/main.cu:1545-1563):
+// larger power wins, equal power -> lower index (the first maximum).
+__device__ __forceinline__ bool better(double p1, uint32_t k1, double p2, uint32_t k2) {
+    return p1 > p2 || (p1 == p2 && k1 < k2);
+}
+
+template <int NT>
+__device__ __forceinline__ void block_best(double &bp, uint32_t &bk, double *s_p, uint32_t *s_k) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double op = __shfl_xor_sync(0xffffffffu, bp, o);
+        const uint32_t ok = __shfl_xor_sync(0xffffffffu, bk, o);
+        if (better(op, ok, bp, bk)) { bp = op; bk = ok; }
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) { s_p[w] = bp; s_k[w] = bk; }
+    __syncthreads();
+    if (w == 0) {
+        bp = l < NT / 32 ? s_p[l] : 0.0;
+        bk = l < NT / 32 ? s_k[l] : 0xffffffffu;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double op = __shfl_xor_sync(0xffffffffu, bp, o);
+            const uint32_t ok = __shfl_xor_sync(0xffffffffu, bk, o);
+            if (better(op, ok, bp, bk)) { bp = op; bk = ok; }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Per-object statistics (FP64). One CTA per object.
+//  standard: norm = 2 / (N * sigma^2), sigma^2 the population variance of y
+//            (source/main.cu:1295-1317, :1335), or 1 without normalization.
+//  generalized (mixed form only): weighted mean of y with w = 1/dy^2 and the
+//            quantities the mixed kernel needs to undo the float rounding of
+//            the stored weights.
+// ---------------------------------------------------------------------------
+__global__ void stats_kernel(int variant, int mixed, int dtype, int normalize, const void *y,
+                             const void *dy, ObjInfo *objs) {
+    __shared__ double s_red[32];
+    ObjInfo &ob = objs[blockIdx.x];
+    const uint64_t r0 = ob.row0;
+    const uint32_t n = ob.n;
+    if (variant == 0) {
+        double s = 0.0;
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) s += load_in(dtype, y, r0 + i);
+        const double mean = block_sum(s, s_red) / (n * 1.0);
+        double s2 = 0.0;
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+            const double d = load_in(dtype, y, r0 + i) - mean;
+            s2 += d * d;
+        }
+        s2 = block_sum(s2, s_red);
+        if (threadIdx.x == 0) {
+            const double sigma = sqrt(s2 / (n * 1.0));
+            ob.norm = normalize ? 2.0 / (n * (sigma * sigma)) : 1.0;
+        }
+        return;
+    }
+    if (!mixed) {
+        if (threadIdx.x == 0) ob.norm = 1.0;
+        return;
+    }
+    double w_s = 0.0, wy_s = 0.0;
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        double w = 1.0 / load_in(dtype, dy, r0 + i);
+        w = w * w;
+        w_s += w;
+        wy_s += w * load_in(dtype, y, r0 + i);
+    }
+    const double W = block_sum(w_s, s_red);
+    const double ym = block_sum(wy_s, s_red) / W;
+    double wf_s = 0.0, yf_s = 0.0, yy_s = 0.0;
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        double w = 1.0 / load_in(dtype, dy, r0 + i);
+        w = w * w;
+        const double wn = w / W;
+        const double yc = load_in(dtype, y, r0 + i) - ym;
+        wf_s += (double)(float)wn;
+        yf_s += (double)(float)(wn * yc);
+        yy_s += wn * yc * yc;
+    }
+    const double wf = block_sum(wf_s, s_red);
+    const double yf = block_sum(yf_s, s_red);
+    const double yy = block_sum(yy_s, s_red);
+    if (threadIdx.x == 0) {
+        ob.wtot = W;
+        ob.ymean = ym;
+        ob.wsum_f = wf;
+        ob.ybar_f = yf / wf;
+        const double ybar = yf / wf;
+        ob.norm = 1.0 / (yy - ybar * ybar);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Observation records of the mixed kernel (FP64 set-up, once per row).
+// ---------------------------------------------------------------------------
+__global__ void records_kernel(int variant, int dtype, const void *t, const void *y,
+                               const void *dy, const uint64_t *offsets, uint32_t n_obj,
+                               const ObjInfo *objs, uint64_t rows, GridTurns g, ObsRec *rec) {
+    for (uint64_t row = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; row < rows;
+         row += (uint64_t)gridDim.x * blockDim.x) {
+        const double td = load_in(dtype, t, row);
+        const uint64_t a = frac_turns_u64(g.f0_hi, g.f0_lo, td);
+        const uint64_t b = frac_turns_u64(g.df_hi, g.df_lo, td);
+        double sd, cd;
+        sincos((double)(long long)b * kTwoPiOver2p64, &sd, &cd);
+        ObsRec r;
+        r.a_lo = (uint32_t)a;
+        r.a_hi = (uint32_t)(a >> 32);
+        r.b_lo = (uint32_t)b;
+        r.b_hi = (uint32_t)(b >> 32);
+        r.cd = (float)cd;
+        r.sd = (float)sd;
+        if (variant == 0) {
+            r.v0 = (float)load_in(dtype, y, row);
+            r.v1 = 0.0f;
+        } else {
+            // object of this row: last o with offsets[o] <= row
+            uint32_t lo = 0, hi = n_obj;
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (offsets[mid] <= row) lo = mid; else hi = mid;
+            }
+            const ObjInfo &ob = objs[lo];
+            double w = 1.0 / load_in(dtype, dy, row);
+            w = w * w;
+            const double wn = w / ob.wtot;
+            r.v0 = (float)wn;
+            r.v1 = (float)(wn * (load_in(dtype, y, row) - ob.ymean));
+        }
+        reinterpret_cast<uint4 *>(rec + row)[0] = make_uint4(r.a_lo, r.a_hi, r.b_lo, r.b_hi);
+        reinterpret_cast<float4 *>(rec + row)[1] = make_float4(r.v0, r.v1, r.cd, r.sd);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Mixed kernel.
+// ---------------------------------------------------------------------------
+
+// Standard L-S power from the sums of one frequency (N observations):
+//   P = 1/2 [ (Q+U)/(N+r) + (Q-U)/(N-r) ],  Q = XC^2+XS^2,
+//   U = [ (CC-SS)(XC^2-XS^2) + 4 CS XC XS ] / r,  r = hypot(CC-SS, 2 CS),
+// which is source/main.cu:1588-1598 with cos/sin(2 omega tau) = (CC-SS, 2CS)/r.
+// N - r is evaluated as 4 (CC SS - CS^2)/(N + r) to avoid cancellation.
+__device__ __forceinline__ float std_power_f(float N, float xc, float xs, float cc, float cs) {
+    const float ss = N - cc;
+    const float D = cc - ss;
+    const float E = 2.0f * cs;
+    const float r = sqrtf(fmaf(D, D, E * E));
+    const float xc2 = xc * xc, xs2 = xs * xs;
+    const float Q = xc2 + xs2;
+    const float V = xc2 - xs2;
+    const float U = r > 0.0f ? fmaf(D, V, 2.0f * E * xc * xs) / r : V;
+    const float den1 = N + r;
+    const float den2 = 4.0f * fmaf(cc, ss, -cs * cs) / den1;
+    return 0.5f * ((Q + U) / den1 + (Q - U) / den2);
+}
+
+// Generalized (floating-mean) power from weighted sums with total weight W:
+// the same closed form applied to the weighted covariances, which is
+// source/main.cu:1728-1776 with the second pass expressed by rotating the
+// first-pass sums by omega*tau.
+__device__ __forceinline__ float gen_power_f(float invW, float ybar, float C, float S, float YC,
+                                             float YS, float CC, float CS) {
+    const float cb = C * invW, sb = S * invW;
+    const float cc = CC * invW, cs = CS * invW;
+    const float ss = 1.0f - cc;
+    const float yc = fmaf(-ybar, cb, YC * invW);
+    const float ys = fmaf(-ybar, sb, YS * invW);
+    const float vcc = fmaf(-cb, cb, cc);
+    const float vss = fmaf(-sb, sb, ss);
+    const float vcs = fmaf(-cb, sb, cs);
+    const float D = vcc - vss, E = 2.0f * vcs, T = vcc + vss;
+    const float r = sqrtf(fmaf(D, D, E * E));
+    const float yc2 = yc * yc, ys2 = ys * ys;
+    const float Q = yc2 + ys2, V = yc2 - ys2;
+    const float U = r > 0.0f ? fmaf(D, V, 2.0f * E * yc * ys) / r : V;
+    const float den1 = T + r;
+    const float den2 = 4.0f * fmaf(vcc, vss, -vcs * vcs) / den1;
+    return (Q + U) / den1 + (Q - U) / den2;
+}
+
+template <typename OutT>
+__device__ __forceinline__ void store_out(void *pgram, uint64_t i, float p) {
+    reinterpret_cast<OutT *>(pgram)[i] = (OutT)p;
+}
+template <typename OutT>
+__device__ __forceinline__ void store_out_d(void *pgram, uint64_t i, double p) {
+    reinterpret_cast<OutT *>(pgram)[i] = (OutT)p;
+}
+
+template <int F, int NT, bool GEN, typename OutT>
+__global__ void __launch_bounds__(NT, 2) mixed_kernel(MixedArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    uint4 *s_rec = reinterpret_cast<uint4 *>(smem_raw);  // 2 x uint4 per observation
+    __shared__ uint32_t s_unit;
+    __shared__ double s_bp[NT / 32];
+    __shared__ uint32_t s_bk[NT / 32];
+    constexpr int NA = GEN ? 6 : 4;
+    const uint32_t units = a.n_obj * a.n_tiles;
+
+    for (;;) {
+        if (threadIdx.x == 0) s_unit = atomicAdd(a.counter, 1u);
+        __syncthreads();
+        const uint32_t u = s_unit;
+        if (u >= units) break;
+        const uint32_t o = a.perm[u / a.n_tiles];
+        const uint32_t tile = u - (u / a.n_tiles) * a.n_tiles;
+        const uint64_t row0 = a.objs[o].row0;
+        const uint32_t n = a.objs[o].n;
+        const uint32_t k0 = tile * (uint32_t)(NT * F) + threadIdx.x * (uint32_t)F;
+
+        float acc[NA][F];
+#pragma unroll
+        for (int q = 0; q < NA; ++q)
+#pragma unroll
+            for (int f = 0; f < F; ++f) acc[q][f] = 0.0f;
+
+        for (uint32_t c0 = 0; c0 < n; c0 += a.chunk) {
+            const uint32_t cnt = min(a.chunk, n - c0);
+            const uint4 *src = reinterpret_cast<const uint4 *>(a.rec + row0 + c0);
+            for (uint32_t i = threadIdx.x; i < 2 * cnt; i += NT) s_rec[i] = __ldg(src + i);
+            __syncthreads();
+#pragma unroll 1
+            for (uint32_t j = 0; j < cnt; ++j) {
+                const uint4 ab = s_rec[2 * j];
+                const float4 v = reinterpret_cast<const float4 *>(s_rec)[2 * j + 1];
+                // anchor: top 32 bits of a + k0*b (mod 2^64), as a signed turn count
+                const uint64_t p = (uint64_t)k0 * ab.z + (((uint64_t)ab.y << 32) | ab.x);
+                const uint32_t hi = (uint32_t)(p >> 32) + k0 * ab.w;
+                float s, c;
+                __sincosf((float)(int32_t)hi * kTwoPiOver2p32f, &s, &c);
+#pragma unroll
+                for (int f = 0; f < F; ++f) {
+                    if (!GEN) {
+                        acc[0][f] = fmaf(v.x, c, acc[0][f]);  // XC
+                        acc[1][f] = fmaf(v.x, s, acc[1][f]);  // XS
+                        acc[2][f] = fmaf(c, c, acc[2][f]);    // CC
+                        acc[3][f] = fmaf(c, s, acc[3][f]);    // CS
+                    } else {
+                        const float wc = v.x * c;
+                        acc[0][f] += wc;                       // C
+                        acc[1][f] = fmaf(v.x, s, acc[1][f]);   // S
+                        acc[2][f] = fmaf(v.y, c, acc[2][f]);   // YC
+                        acc[3][f] = fmaf(v.y, s, acc[3][f]);   // YS
+                        acc[4][f] = fmaf(wc, c, acc[4][f]);    // CC
+                        acc[5][f] = fmaf(wc, s, acc[5][f]);    // CS
+                    }
+                    if (f + 1 < F) {
+                        const float cn = fmaf(c, v.z, -s * v.w);
+                        s = fmaf(s, v.z, c * v.w);
+                        c = cn;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+
+        // epilogue: power, optional store, thread-local first maximum
+        double bp = 0.0;
+        uint32_t bk = 0xffffffffu;
+        if (tile == 0 && threadIdx.x == 0) bk = 0;  // the reference's (power 0, index 0) start
+        const uint64_t out0 = (uint64_t)o * a.n_freq;
+        if (!GEN) {
+            const float N = (float)n;
+            const float nrm = (float)a.objs[o].norm;
+#pragma unroll
+            for (int f = 0; f < F; ++f) {
+                const uint32_t k = k0 + f;
+                const float P = std_power_f(N, acc[0][f], acc[1][f], acc[2][f], acc[3][f]) * nrm;
+                if (k < a.n_freq) {
+                    if (a.pgram) store_out<OutT>(a.pgram, out0 + k, P);
+                    if ((double)P > bp) { bp = (double)P; bk = k; }
+                }
+            }
+        } else {
+            const float invW = (float)(1.0 / a.objs[o].wsum_f);
+            const float ybar = (float)a.objs[o].ybar_f;
+            const float nrm = (float)a.objs[o].norm;
+#pragma unroll
+            for (int f = 0; f < F; ++f) {
+                const uint32_t k = k0 + f;
+                const float P = gen_power_f(invW, ybar, acc[0][f], acc[1][f], acc[2][f], acc[3][f],
+                                            acc[4][f], acc[5][f]) * nrm;
+                if (k < a.n_freq) {
+                    if (a.pgram) store_out<OutT>(a.pgram, out0 + k, P);
+                    if ((double)P > bp) { bp = (double)P; bk = k; }
+                }
+            }
+        }
+        if (a.tile_best) {
+            block_best<NT>(bp, bk, s_bp, s_bk);
+            if (threadIdx.x == 0) {
+                TileBest tb;
+                tb.p = bp;
+                tb.k = bk;
+                tb.pad = 0;
+                a.tile_best[(uint64_t)o * a.n_tiles + tile] = tb;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Plain FP64 kernel: the reference's arithmetic, one frequency per thread.
+// ---------------------------------------------------------------------------
+template <int NT, bool GEN, typename InT, typename OutT>
+__global__ void __launch_bounds__(NT) plain_kernel(PlainArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double *s_t = reinterpret_cast<double *>(smem_raw);
+    double *s_y = s_t + a.chunk;
+    double *s_w = s_y + a.chunk;  // generalized only
+    __shared__ uint32_t s_unit;
+    __shared__ double s_bp[NT / 32];
+    __shared__ uint32_t s_bk[NT / 32];
+    const InT *T = reinterpret_cast<const InT *>(a.t);
+    const InT *Y = reinterpret_cast<const InT *>(a.y);
+    const InT *DY = reinterpret_cast<const InT *>(a.dy);
+    const uint32_t units = a.n_obj * a.n_tiles;
+
+    for (;;) {
+        if (threadIdx.x == 0) s_unit = atomicAdd(a.counter, 1u);
+        __syncthreads();
+        const uint32_t u = s_unit;
+        if (u >= units) break;
+        const uint32_t o = a.perm[u / a.n_tiles];
+        const uint32_t tile = u - (u / a.n_tiles) * a.n_tiles;
+        const uint64_t row0 = a.objs[o].row0;
+        const uint32_t n = a.objs[o].n;
+        const uint32_t k = tile * (uint32_t)NT + threadIdx.x;
+        // source/main.cu:1611 / source/kernel.cu:538: omega = minFreq + freqStep*k
+        const double w = a.fmin + (a.df * (double)k);
+        double P;
+        if (!GEN) {
+            double xc = 0.0, xs = 0.0, cc = 0.0, ss = 0.0, cs = 0.0;
+            for (uint32_t c0 = 0; c0 < n; c0 += a.chunk) {
+                const uint32_t cnt = min(a.chunk, n - c0);
+                for (uint32_t i = threadIdx.x; i < cnt; i += NT) {
+                    s_t[i] = (double)T[row0 + c0 + i];
+                    s_y[i] = (double)Y[row0 + c0 + i];
+                }
+                __syncthreads();
+#pragma unroll 2
+                for (uint32_t j = 0; j < cnt; ++j) {
+                    double s, c;
+                    sincos(w * s_t[j], &s, &c);
+                    const double yj = s_y[j];
+                    xc += yj * c;
+                    xs += yj * s;
+                    cc += c * c;
+                    ss += s * s;
+                    cs += c * s;
+                }
+                __syncthreads();
+            }
+            // source/main.cu:1588-1598
+            const double tau = atan2(2.0 * cs, cc - ss) / (2.0 * w);
+            double s_tau, c_tau;
+            sincos(w * tau, &s_tau, &c_tau);
+            const double c_tau2 = c_tau * c_tau, s_tau2 = s_tau * s_tau;
+            const double cs_tau = 2.0 * c_tau * s_tau;
+            const double f1 = c_tau * xc + s_tau * xs;
+            const double f2 = c_tau * xs - s_tau * xc;
+            P = 0.5 * ((f1 * f1) / (c_tau2 * cc + cs_tau * cs + s_tau2 * ss) +
+                       (f2 * f2) / (c_tau2 * ss - cs_tau * cs + s_tau2 * cc));
+            P *= a.objs[o].norm;
+        } else {
+            // source/main.cu:1701-1777 (two passes over the observations)
+            double wsum = 0.0, S = 0.0, C = 0.0, S2 = 0.0, C2 = 0.0;
+            const bool one_chunk = n <= a.chunk;
+            for (int pass = 0; pass < 2; ++pass) {
+                double tau = 0.0;
+                if (pass == 1) {
+                    S2 /= wsum;
+                    C2 /= wsum;
+                    S /= wsum;
+                    C /= wsum;
+                    S2 -= (2.0 * S * C);
+                    C2 -= (C * C - S * S);
+                    tau = 0.5 * atan2(S2, C2) / w;
+                }
+                double Y_ = 0.0, YY = 0.0, Ct = 0.0, St = 0.0, YCt = 0.0, YSt = 0.0, CCt = 0.0,
+                       SSt = 0.0;
+                for (uint32_t c0 = 0; c0 < n; c0 += a.chunk) {
+                    const uint32_t cnt = min(a.chunk, n - c0);
+                    if (!(one_chunk && pass == 1)) {
+                        for (uint32_t i = threadIdx.x; i < cnt; i += NT) {
+                            s_t[i] = (double)T[row0 + c0 + i];
+                            s_y[i] = (double)Y[row0 + c0 + i];
+                            double wi = 1.0 / (double)DY[row0 + c0 + i];
+                            s_w[i] = wi * wi;
+                        }
+                        __syncthreads();
+                    }
+                    if (pass == 0) {
+#pragma unroll 2
+                        for (uint32_t j = 0; j < cnt; ++j) {
+                            const double wj = s_w[j];
+                            double s, c;
+                            sincos(w * s_t[j], &s, &c);
+                            wsum += wj;
+                            S += wj * s;
+                            C += wj * c;
+                            S2 += 2.0 * wj * s * c;
+                            C2 += wj - 2.0 * wj * s * s;
+                        }
+                    } else {
+#pragma unroll 2
+                        for (uint32_t j = 0; j < cnt; ++j) {
+                            const double wj = s_w[j], yj = s_y[j];
+                            double s, c;
+                            sincos(w * (s_t[j] - tau), &s, &c);
+                            Y_ += wj * yj;
+                            YY += wj * yj * yj;
+                            Ct += wj * c;
+                            St += wj * s;
+                            YCt += wj * yj * c;
+                            YSt += wj * yj * s;
+                            CCt += wj * c * c;
+                            SSt += wj * s * s;
+                        }
+                    }
+                    if (!(one_chunk && pass == 0)) __syncthreads();
+                }
+                if (pass == 1) {
+                    Y_ /= wsum;
+                    YY /= wsum;
+                    Ct /= wsum;
+                    St /= wsum;
+                    YCt /= wsum;
+                    YSt /= wsum;
+                    CCt /= wsum;
+                    SSt /= wsum;
+                    YCt -= Y_ * Ct;
+                    YSt -= Y_ * St;
+                    CCt -= Ct * Ct;
+                    SSt -= St * St;
+                    YY -= Y_ * Y_;
+                    P = (YCt * YCt / CCt + YSt * YSt / SSt) / YY;
+                }
+            }
+        }
+        double bp = 0.0;
+        uint32_t bk = 0xffffffffu;
+        if (tile == 0 && threadIdx.x == 0) bk = 0;
+        if (k < a.n_freq) {
+            if (a.pgram) store_out_d<OutT>(a.pgram, (uint64_t)o * a.n_freq + k, P);
+            const double Pr = (double)(OutT)P;  // compare in the output precision
+            if (Pr > bp) { bp = Pr; bk = k; }
+        }
+        if (a.tile_best) {
+            block_best<NT>(bp, bk, s_bp, s_bk);
+            if (threadIdx.x == 0) {
+                TileBest tb;
+                tb.p = bp;
+                tb.k = bk;
+                tb.pad = 0;
+                a.tile_best[(uint64_t)o * a.n_tiles + tile] = tb;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Per-object argmax over the tile results, tiles in frequency order, first
+// maximum wins; one warp per object.
+// ---------------------------------------------------------------------------
+template <typename OutT>
+__global__ void best_reduce_kernel(const TileBest *tb, uint32_t n_obj, uint32_t n_tiles,
+                                   uint32_t *best_idx, OutT *best_power) {
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= n_obj) return;
+    double bp = 0.0;
+    uint32_t bk = 0xffffffffu;
+    for (uint32_t i = lane; i < n_tiles; i += 32) {
+        const TileBest x = tb[(uint64_t)warp * n_tiles + i];
+        if (better(x.p, x.k, bp, bk)) { bp = x.p; bk = x.k; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double op = __shfl_xor_sync(0xffffffffu, bp, o);
+        const uint32_t ok = __shfl_xor_sync(0xffffffffu, bk, o);
+        if (better(op, ok, bp, bk)) { bp = op; bk = ok; }
+    }
+    if (lane == 0) {
+        if (best_idx) best_idx[warp] = bk == 0xffffffffu ? 0u : bk;
+        if (best_power) best_power[warp] = (OutT)bp;
+    }
+}
+
+template <int F, int NT, bool GEN>
+cudaError_t launch_mixed_t(int dtype, const MixedArgs &a, int grid, size_t smem, cudaStream_t st) {
+    if (dtype == 0) {
+        auto k = mixed_kernel<F, NT, GEN, float>;
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k<<<grid, NT, smem, st>>>(a);
+    } else {
+        auto k = mixed_kernel<F, NT, GEN, double>;
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k<<<grid, NT, smem, st>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+template <int F, int NT, bool GEN>
+cudaError_t occ_mixed_t(int dtype, size_t smem, int *blocks) {
+    cudaError_t e;
+    if (dtype == 0) {
+        auto k = mixed_kernel<F, NT, GEN, float>;
+        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k, NT, smem);
+    } else {
+        auto k = mixed_kernel<F, NT, GEN, double>;
+        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k, NT, smem);
+    }
+    return e;
+}
+
+// The compiled mixed shapes. Keep in sync with kMixedShapes in lsgb_engine.cu.
+#define LSGB_MIXED_SHAPES(X) \
+    X(16, 256, false)        \
+    X(8, 256, false)         \
+    X(8, 128, false)         \
+    X(4, 256, false)         \
+    X(8, 256, true)          \
+    X(4, 256, true)          \
+    X(12, 256, true)
+
+}  // namespace
+
+cudaError_t launch_stats(int variant, int mixed, int dtype, int normalize, const void *y,
+                         const void *dy, ObjInfo *objs, uint32_t n_obj, cudaStream_t st) {
+    if (n_obj == 0) return cudaSuccess;
+    stats_kernel<<<n_obj, 256, 0, st>>>(variant, mixed, dtype, normalize, y, dy, objs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_records(int variant, int dtype, const void *t, const void *y, const void *dy,
+                           const uint64_t *offsets, uint32_t n_obj, const ObjInfo *objs,
+                           uint64_t rows, GridTurns g, ObsRec *rec, cudaStream_t st) {
+    if (rows == 0) return cudaSuccess;
+    const uint64_t blocks64 = (rows + 255) / 256;
+    const int blocks = (int)(blocks64 < 65535ull * 16 ? blocks64 : 65535ull * 16);
+    records_kernel<<<blocks, 256, 0, st>>>(variant, dtype, t, y, dy, offsets, n_obj, objs, rows, g,
+                                           rec);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mixed(int variant, int dtype, MixedShape shape, const MixedArgs &a, int grid,
+                         size_t smem, cudaStream_t st) {
+#define X(F_, NT_, G_)                                                   \
+    if (shape.f == F_ && shape.nt == NT_ && (variant == 1) == G_)        \
+        return launch_mixed_t<F_, NT_, G_>(dtype, a, grid, smem, st);
+    LSGB_MIXED_SHAPES(X)
+#undef X
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t mixed_occupancy(int variant, int dtype, MixedShape shape, size_t smem, int *blocks) {
+#define X(F_, NT_, G_)                                            \
+    if (shape.f == F_ && shape.nt == NT_ && (variant == 1) == G_) \
+        return occ_mixed_t<F_, NT_, G_>(dtype, smem, blocks);
+    LSGB_MIXED_SHAPES(X)
+#undef X
+    return cudaErrorInvalidValue;
+}
+
+namespace {
+template <bool GEN, typename InT, typename OutT>
+cudaError_t plain_t(const PlainArgs &a, int grid, size_t smem, cudaStream_t st, int *occ) {
+    auto k = plain_kernel<kPlainThreads, GEN, InT, OutT>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, k, kPlainThreads, smem);
+    k<<<grid, kPlainThreads, smem, st>>>(a);
+    return cudaGetLastError();
+}
+template <bool GEN>
+cudaError_t plain_dispatch(int in_dtype, int out_dtype, const PlainArgs &a, int grid, size_t smem,
+                           cudaStream_t st, int *occ) {
+    if (in_dtype == 0 && out_dtype == 0) return plain_t<GEN, float, float>(a, grid, smem, st, occ);
+    if (in_dtype == 0 && out_dtype == 1) return plain_t<GEN, float, double>(a, grid, smem, st, occ);
+    if (in_dtype == 1 && out_dtype == 0) return plain_t<GEN, double, float>(a, grid, smem, st, occ);
+    return plain_t<GEN, double, double>(a, grid, smem, st, occ);
+}
+}  // namespace
+
+cudaError_t launch_plain(int variant, int in_dtype, int out_dtype, const PlainArgs &a, int grid,
+                         size_t smem, cudaStream_t st) {
+    return variant == 0 ? plain_dispatch<false>(in_dtype, out_dtype, a, grid, smem, st, nullptr)
+                        : plain_dispatch<true>(in_dtype, out_dtype, a, grid, smem, st, nullptr);
+}
+
+cudaError_t plain_occupancy(int variant, int in_dtype, int out_dtype, size_t smem, int *blocks) {
+    PlainArgs dummy{};
+    return variant == 0 ? plain_dispatch<false>(in_dtype, out_dtype, dummy, 0, smem, 0, blocks)
+                        : plain_dispatch<true>(in_dtype, out_dtype, dummy, 0, smem, 0, blocks);
+}
+
+cudaError_t launch_best_reduce(int dtype, const TileBest *tb, uint32_t n_obj, uint32_t n_tiles,
+                               uint32_t *best_idx, void *best_power, cudaStream_t st) {
+    if (n_obj == 0) return cudaSuccess;
+    const int threads = 256;
+    const int blocks = (int)((n_obj * 32ull + threads - 1) / threads);
+    if (dtype == 0)
+        best_reduce_kernel<float><<<blocks, threads, 0, st>>>(tb, n_obj, n_tiles, best_idx,
+                                                              (float *)best_power);
+    else
+        best_reduce_kernel<double><<<blocks, threads, 0, st>>>(tb, n_obj, n_tiles, best_idx,
+                                                               (double *)best_power);
+    return cudaGetLastError();
+}
+
+}  // namespace lsgb

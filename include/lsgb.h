@@ -1,0 +1,110 @@
+/*
+ * lsgb.h -- C ABI of the GB300 Lomb-Scargle engine (liblsgb.so).
+ *
+ * Plain pointers and sizes only. Every call returns LSGB_OK (0) or a negative
+ * status; lsgb_last_error() gives the message of the last failure on the calling
+ * thread. Nothing here exits the process.
+ *
+ * Work model. A batch is n_obj objects whose observations are the rows
+ * [offsets[o], offsets[o+1]) of the arrays t, y, dy (the reference's contiguous
+ * object runs, source/main.cu:468-510 computeObjectRanges, expressed as offsets).
+ * The frequency grid is angular, omega_k = fmin + df * k, k = 0..n_freq-1
+ * (source/main.cu:1364, :1609-1611).
+ *
+ * Each entry point below replaces part of the reference's GPU path:
+ *   lsgb_periodogram_device  -> source/main.cu:1006-1280 batchGPULS (and :570-720
+ *                               GPULSOneObject for n_obj == 1) without its per-call
+ *                               cudaMalloc/cudaFree, host argmax or forced pgram copy;
+ *                               kernels source/kernel.cu:368-631 and :76-361.
+ *   lsgb_periodogram_host    -> the same behind host buffers, including the copies
+ *                               (source/main.cu:1070-1077 H2D, :1100-1110 D2H).
+ * The reference-compatible entry point LombScarglePy is declared in lombscargle_py.h.
+ */
+#ifndef LSGB_H
+#define LSGB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LSGB_API __attribute__((visibility("default")))
+
+/* status codes */
+#define LSGB_OK 0
+#define LSGB_ERR_INVALID (-1)   /* bad argument: sizes, offsets, enum values */
+#define LSGB_ERR_CUDA (-2)      /* a CUDA call failed (message names it) */
+#define LSGB_ERR_NOMEM (-3)     /* device or pinned allocation failed */
+#define LSGB_ERR_NODEVICE (-4)  /* no CUDA device: the engine never computes on the CPU */
+
+/* variant: the reference's ERROR compile flag (source/params.h:12-16) */
+#define LSGB_STANDARD 0     /* ERROR=0: standard L-S, source/kernel.cu:484-631 */
+#define LSGB_GENERALIZED 1  /* ERROR=1: floating mean + 1/dy^2 weights, source/kernel.cu:368-477 */
+
+/* precision form */
+#define LSGB_PLAIN_FP64 0 /* FP64 sincos for every pair, FP64 atan2 tau: the drop-in form */
+#define LSGB_MIXED 1      /* FP64 phase anchors + FP32 angle-addition recurrence */
+
+/* element type of t / y / dy / pgram / best_power */
+#define LSGB_F32 0
+#define LSGB_F64 1
+
+typedef struct lsgb_engine lsgb_engine;
+
+/* Create an engine bound to a CUDA device. The engine owns grow-only device
+ * scratch buffers reused by every call. Calls on one engine must be issued from
+ * one host thread at a time and ordered on one stream. */
+LSGB_API int lsgb_engine_create(int device, lsgb_engine **out);
+LSGB_API void lsgb_engine_destroy(lsgb_engine *eng);
+LSGB_API const char *lsgb_last_error(void);
+LSGB_API const char *lsgb_version(void);
+
+/* Periodograms of a batch, inputs and outputs in device memory.
+ *   t, y, dy     device arrays of offsets_host[n_obj] rows (dtype); dy may be NULL
+ *                for LSGB_STANDARD.
+ *   offsets_host host array of n_obj+1 non-decreasing row offsets, offsets[0] == 0;
+ *                every object must have at least one row.
+ *   normalize    LSGB_STANDARD only: multiply by 2/(N*var(y)) as the Python builds do
+ *                (source/main.cu:1319-1352, -DNORMALIZEPGRAM=1).
+ *   pgram        device [n_obj x n_freq] (dtype) or NULL: full periodogram.
+ *   best_idx     device uint32[n_obj] or NULL: first index of the maximum power,
+ *                0 when no power is positive (source/main.cu:1545-1563).
+ *   best_power   device [n_obj] (dtype) or NULL: that power (0 when none).
+ *   stream       cudaStream_t (NULL = legacy default stream).
+ * Asynchronous with respect to the host. */
+LSGB_API int lsgb_periodogram_device(lsgb_engine *eng, int variant, int precision, int dtype,
+                                     const void *t, const void *y, const void *dy,
+                                     const uint64_t *offsets_host, uint32_t n_obj, double fmin,
+                                     double df, uint32_t n_freq, int normalize, void *pgram,
+                                     uint32_t *best_idx, void *best_power, void *stream);
+
+/* The same with host buffers (pinned or pageable). Copies the inputs in, computes,
+ * copies pgram (if non-NULL) and the best index/power (if non-NULL) out, and
+ * returns when they are in host memory. */
+LSGB_API int lsgb_periodogram_host(lsgb_engine *eng, int variant, int precision, int dtype,
+                                   const void *t, const void *y, const void *dy,
+                                   const uint64_t *offsets, uint32_t n_obj, double fmin, double df,
+                                   uint32_t n_freq, int normalize, void *pgram, uint32_t *best_idx,
+                                   void *best_power);
+
+/* Tuning of the mixed kernel: frequencies per thread (F) and threads per CTA.
+ * 0 keeps the built-in choice. Returns LSGB_ERR_INVALID for shapes that are not
+ * compiled in. */
+LSGB_API int lsgb_set_tuning(lsgb_engine *eng, int variant, int freqs_per_thread,
+                             int threads_per_cta);
+
+/* Launch statistics of the last call: kernels launched and the work units the
+ * persistent kernel processed. */
+LSGB_API int lsgb_last_launch_info(lsgb_engine *eng, uint32_t *kernels_launched,
+                                   uint64_t *work_units);
+
+/* Device time (ms) of the last main (periodogram) kernel launch, measured with
+ * CUDA events recorded around it on the call's stream; waits for it to finish. */
+LSGB_API int lsgb_last_kernel_time(lsgb_engine *eng, float *ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LSGB_H */

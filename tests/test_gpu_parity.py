@@ -1,0 +1,188 @@
+"""GPU parity of the engine (through the lsgb_* C ABI) against the oracle.
+
+Plain FP64 form: <= 1e-9 relative per frequency and identical best periods.
+Mixed form: <= 1e-4 absolute normalized power and identical best periods (except
+top-two ties within the tolerance). See tests/gpu_helpers.py.
+"""
+import numpy as np
+import pytest
+
+from gpu_lomb_scargle_gb300 import engine as E
+from gpu_lomb_scargle_gb300 import synth
+from oracle import pyoracle
+from tests.gpu_helpers import MIXED_ATOL, PLAIN_RTOL, check_best, mixed_abs_err, plain_rel_err
+
+pytestmark = pytest.mark.gpu
+TWO_PI = 2.0 * np.pi
+
+
+@pytest.fixture(scope="module")
+def eng(native_libs, cuda_ok):
+    return E.Engine(0)
+
+
+def one(n):
+    return np.array([0, n], np.uint64)
+
+
+def offs_of(ids):
+    return E.offsets_from_ids(ids)
+
+
+# ---------------------------------------------------------------- fixtures of the reference
+@pytest.mark.parametrize("variant,tag", [(0, "8205_std"), (1, "8205_gen")])
+def test_plain_matches_reference_cpu_8205(eng, golden, variant, tag):
+    lo, hi, nf = golden["8205_grid"]
+    nf = int(nf)
+    t, dy = golden[tag + "_t"], golden[tag + "_dy"]
+    # the reference pre-centers y before its generalized loops: use its mutated y
+    y = golden[tag + "_double_yafter"] if variant == 1 else golden[tag + "_y"]
+    r = eng.run_host(variant, "plain", t, y, dy if variant else None, one(t.size), lo,
+                     (hi - lo) / nf, nf, normalize=(variant == 0), want_pgram=True)
+    ref = golden[tag + "_double_pgram"]
+    err = plain_rel_err(r.pgram[0], ref)
+    print(f"{tag} plain rel err {err:.3g}")
+    assert err < PLAIN_RTOL
+    assert int(r.best_idx[0]) == int(np.argmax(ref))
+    assert r.best_power[0] == r.pgram[0][r.best_idx[0]]
+
+
+@pytest.mark.parametrize("variant,tag", [(0, "batch_std"), (1, "batch_gen")])
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+def test_batch_matches_reference_cpu(eng, golden, variant, tag, precision):
+    lo, hi, nf = golden[tag + "_grid"]
+    nf = int(nf)
+    ids = golden[tag + "_ids"]
+    y = golden[tag + "_double_yafter"] if variant == 1 else golden[tag + "_y"]
+    r = eng.run_host(variant, precision, golden[tag + "_t"], y, golden[tag + "_dy"], offs_of(ids),
+                     lo, (hi - lo) / nf, nf, normalize=(variant == 0), want_pgram=True)
+    ref = golden[tag + "_double_pgram"]
+    if precision == "plain":
+        err = plain_rel_err(r.pgram, ref)
+        print(f"{tag} plain rel err {err:.3g}")
+        assert err < PLAIN_RTOL
+        assert check_best(r.best_idx, ref) == []
+    else:
+        err = mixed_abs_err(r.pgram, ref)
+        print(f"{tag} mixed abs err {err:.3g}")
+        assert err < MIXED_ATOL
+        assert check_best(r.best_idx, ref, tol=MIXED_ATOL) == []
+
+
+def test_known_answer_243_plain(eng, golden):
+    """JD-scale times (2.4587e6 d): P = 0.096536 (README.md:92) on the full 1e6 grid."""
+    t, y = golden["243_t"], golden["243_y"]
+    lo, hi, nf = 3.142, 150.796, 1_000_000
+    r = eng.run_host(0, "plain", t, y, None, one(t.size), lo, (hi - lo) / nf, nf, want_pgram=True)
+    k = int(r.best_idx[0])
+    assert k == int(golden["243_1e6_argmax"][0])
+    assert round(TWO_PI / (lo + k * (hi - lo) / nf), 6) == 0.096536
+    start = int(golden["243_1e6_window_start"][0])
+    win = golden["243_1e6_window"]
+    assert plain_rel_err(r.pgram[0][start:start + win.size], win) < PLAIN_RTOL
+
+
+def test_known_answer_243_mixed(eng, golden):
+    t, y = golden["243_t"], golden["243_y"]
+    lo, hi, nf = 3.142, 150.796, 1_000_000
+    r = eng.run_host(0, "mixed", t, y, None, one(t.size), lo, (hi - lo) / nf, nf, want_pgram=True)
+    start = int(golden["243_1e6_window_start"][0])
+    win = golden["243_1e6_window"]
+    assert mixed_abs_err(r.pgram[0][start:start + win.size], win) < MIXED_ATOL
+    assert round(TWO_PI / (lo + int(r.best_idx[0]) * (hi - lo) / nf), 6) == 0.096536
+
+
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+def test_known_answer_8205_generalized_1e6(eng, golden, precision):
+    t, dy = golden["8205_gen_t"], golden["8205_gen_dy"]
+    y = golden["8205_gen_double_yafter"]
+    lo, hi, nf = 3.14159, 150.79645, 1_000_000
+    r = eng.run_host(1, precision, t, y, dy, one(t.size), lo, (hi - lo) / nf, nf, normalize=False,
+                     want_pgram=True)
+    k = int(r.best_idx[0])
+    assert k == int(golden["8205_gen_1e6_argmax"][0])
+    assert round(TWO_PI / (lo + k * (hi - lo) / nf), 6) == 0.564736
+    assert round(float(r.best_power[0]), 4 if precision == "mixed" else 6) == round(0.712905, 4 if precision == "mixed" else 6)
+    start = int(golden["8205_gen_1e6_window_start"][0])
+    win = golden["8205_gen_1e6_window"]
+    seg = r.pgram[0][start:start + win.size]
+    if precision == "plain":
+        assert plain_rel_err(seg, win) < PLAIN_RTOL
+    else:
+        assert mixed_abs_err(seg, win) < MIXED_ATOL
+
+
+# ---------------------------------------------------------------- edge shapes vs the oracle
+EDGE_SIZES = [2, 3, 31, 32, 33, 511, 513, 2047, 2048, 2049, 4100]
+
+
+@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+@pytest.mark.parametrize("n_freq", [1, 7, 255, 4097])
+def test_edge_shapes(eng, variant, precision, n_freq):
+    rng = np.random.default_rng(11 + variant + n_freq)
+    sizes = np.array(EDGE_SIZES)
+    ids = np.repeat(np.arange(sizes.size), sizes).astype(np.uint32)
+    t = np.concatenate([np.sort(rng.uniform(0, 1800, n)) for n in sizes])
+    y = np.concatenate([np.sin(t_ * 0) + rng.normal(0, 1, t_.size) for t_ in np.split(t, np.cumsum(sizes)[:-1])])
+    y += 0.8 * np.sin(TWO_PI * t / 0.37)
+    dy = rng.uniform(0.01, 0.1, t.size)
+    offs = offs_of(ids)
+    lo, hi = 1.005, 150.796
+    df = (hi - lo) / n_freq
+    if variant == 1:
+        _, y = pyoracle.batch_pgram(1, t, y, dy, offs, lo, df, n_freq=1)  # reference pre-centering
+    ref, _ = pyoracle.batch_pgram(variant, t, y, dy, offs, lo, df, n_freq=n_freq)
+    r = eng.run_host(variant, precision, t, y, dy if variant else None, offs, lo, df, n_freq,
+                     normalize=(variant == 0), want_pgram=True)
+    keep = sizes >= 3  # two observations give exactly degenerate denominators (NaN / inf)
+    if precision == "plain":
+        assert plain_rel_err(r.pgram[keep], ref[keep]) < PLAIN_RTOL
+        assert check_best(r.best_idx[keep], ref[keep]) == []
+    else:
+        big = sizes >= 31
+        assert mixed_abs_err(r.pgram[big], ref[big]) < MIXED_ATOL
+        assert check_best(r.best_idx[big], ref[big], tol=MIXED_ATOL) == []
+
+
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+def test_float_inputs_and_outputs(eng, precision):
+    """float32 arrays (the float builds): compare with the FP64 oracle on the same
+    float-rounded inputs."""
+    w = synth.lognormal_batch(seed=99, n_obj=20, n_freq=3000)
+    t = w.t.astype(np.float32)
+    y = w.y.astype(np.float32)
+    ref, _ = pyoracle.batch_pgram(0, t.astype(np.float64), y.astype(np.float64), None, w.offsets,
+                                  w.fmin, w.df, n_freq=w.n_freq)
+    r = eng.run_host(0, precision, t, y, None, w.offsets, w.fmin, w.df, w.n_freq, want_pgram=True)
+    assert r.pgram.dtype == np.float32
+    tol = MIXED_ATOL if precision == "mixed" else 1e-6  # plain: FP64 math, float32 output
+    assert mixed_abs_err(r.pgram, ref) < tol
+    assert check_best(r.best_idx, ref, tol=tol) == []
+
+
+def test_no_pgram_requested_gives_same_best(eng):
+    w = synth.lognormal_batch(seed=5, n_obj=50, n_freq=20000)
+    a = eng.run_host(0, "mixed", w.t, w.y, None, w.offsets, w.fmin, w.df, w.n_freq, want_pgram=True)
+    b = eng.run_host(0, "mixed", w.t, w.y, None, w.offsets, w.fmin, w.df, w.n_freq, want_pgram=False)
+    assert np.array_equal(a.best_idx, b.best_idx)
+    assert np.array_equal(a.best_power, b.best_power)
+    assert np.array_equal(a.best_idx, np.argmax(a.pgram, axis=1))
+
+
+def test_device_api_matches_host_api(eng):
+    import torch
+    w = synth.lognormal_batch(seed=6, n_obj=30, n_freq=5000)
+    h = eng.run_host(0, "mixed", w.t, w.y, None, w.offsets, w.fmin, w.df, w.n_freq, want_pgram=True)
+    dev = torch.device("cuda:0")
+    t = torch.from_numpy(w.t).to(dev)
+    y = torch.from_numpy(w.y).to(dev)
+    pg = torch.empty((w.n_obj, w.n_freq), dtype=torch.float64, device=dev)
+    bi = torch.empty(w.n_obj, dtype=torch.int32, device=dev)
+    bp = torch.empty(w.n_obj, dtype=torch.float64, device=dev)
+    eng.run_device(0, "mixed", t, y, None, w.offsets, w.fmin, w.df, w.n_freq, True, pg, bi, bp)
+    torch.cuda.synchronize()
+    assert np.array_equal(pg.cpu().numpy(), h.pgram)
+    assert np.array_equal(bi.cpu().numpy().astype(np.uint32), h.best_idx)
+    k, units = eng.launch_info()
+    assert k >= 3 and units > 0
