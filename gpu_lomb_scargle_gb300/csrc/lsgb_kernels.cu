@@ -30,7 +30,6 @@ namespace lsgb {
 
 namespace {
 
-constexpr double kTwoPi = 6.283185307179586;
 constexpr double kTwoPiOver2p64 = 3.4061215800865545e-19;  // 2 pi / 2^64
 constexpr float kTwoPiOver2p32f = 1.4629180792671596e-09f;  // 2 pi / 2^32
 constexpr double k2p64 = 18446744073709551616.0;
@@ -222,18 +221,20 @@ __global__ void records_kernel(int variant, int dtype, const void *t, const void
 //   U = [ (CC-SS)(XC^2-XS^2) + 4 CS XC XS ] / r,  r = hypot(CC-SS, 2 CS),
 // which is source/main.cu:1588-1598 with cos/sin(2 omega tau) = (CC-SS, 2CS)/r.
 // N - r is evaluated as 4 (CC SS - CS^2)/(N + r) to avoid cancellation.
+__device__ __forceinline__ float fast_sqrt(float h) { return h > 0.0f ? h * rsqrtf(h) : 0.0f; }
+
 __device__ __forceinline__ float std_power_f(float N, float xc, float xs, float cc, float cs) {
     const float ss = N - cc;
     const float D = cc - ss;
     const float E = 2.0f * cs;
-    const float r = sqrtf(fmaf(D, D, E * E));
+    const float r = fast_sqrt(fmaf(D, D, E * E));
     const float xc2 = xc * xc, xs2 = xs * xs;
     const float Q = xc2 + xs2;
     const float V = xc2 - xs2;
-    const float U = r > 0.0f ? fmaf(D, V, 2.0f * E * xc * xs) / r : V;
+    const float U = r > 0.0f ? __fdividef(fmaf(D, V, 2.0f * E * xc * xs), r) : V;
     const float den1 = N + r;
-    const float den2 = 4.0f * fmaf(cc, ss, -cs * cs) / den1;
-    return 0.5f * ((Q + U) / den1 + (Q - U) / den2);
+    const float den2 = __fdividef(4.0f * fmaf(cc, ss, -cs * cs), den1);
+    return 0.5f * (__fdividef(Q + U, den1) + __fdividef(Q - U, den2));
 }
 
 // Generalized (floating-mean) power from weighted sums with total weight W:
@@ -251,13 +252,13 @@ __device__ __forceinline__ float gen_power_f(float invW, float ybar, float C, fl
     const float vss = fmaf(-sb, sb, ss);
     const float vcs = fmaf(-cb, sb, cs);
     const float D = vcc - vss, E = 2.0f * vcs, T = vcc + vss;
-    const float r = sqrtf(fmaf(D, D, E * E));
+    const float r = fast_sqrt(fmaf(D, D, E * E));
     const float yc2 = yc * yc, ys2 = ys * ys;
     const float Q = yc2 + ys2, V = yc2 - ys2;
-    const float U = r > 0.0f ? fmaf(D, V, 2.0f * E * yc * ys) / r : V;
+    const float U = r > 0.0f ? __fdividef(fmaf(D, V, 2.0f * E * yc * ys), r) : V;
     const float den1 = T + r;
-    const float den2 = 4.0f * fmaf(vcc, vss, -vcs * vcs) / den1;
-    return (Q + U) / den1 + (Q - U) / den2;
+    const float den2 = __fdividef(4.0f * fmaf(vcc, vss, -vcs * vcs), den1);
+    return __fdividef(Q + U, den1) + __fdividef(Q - U, den2);
 }
 
 template <typename OutT>
@@ -409,8 +410,10 @@ __global__ void __launch_bounds__(NT) plain_kernel(PlainArgs a) {
         const uint64_t row0 = a.objs[o].row0;
         const uint32_t n = a.objs[o].n;
         const uint32_t k = tile * (uint32_t)NT + threadIdx.x;
-        // source/main.cu:1611 / source/kernel.cu:538: omega = minFreq + freqStep*k
-        const double w = a.fmin + (a.df * (double)k);
+        // source/main.cu:1611 / source/kernel.cu:538: omega = minFreq + freqStep*k, with the
+        // product rounded before the add as the reference's host code does (a fused
+        // multiply-add would move omega by an ulp: 7e-8 rad of phase at t ~ 2.5e6 d)
+        const double w = __dadd_rn(a.fmin, __dmul_rn(a.df, (double)k));
         double P;
         if (!GEN) {
             double xc = 0.0, xs = 0.0, cc = 0.0, ss = 0.0, cs = 0.0;

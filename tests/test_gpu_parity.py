@@ -135,7 +135,10 @@ def test_edge_shapes(eng, variant, precision, n_freq):
     ref, _ = pyoracle.batch_pgram(variant, t, y, dy, offs, lo, df, n_freq=n_freq)
     r = eng.run_host(variant, precision, t, y, dy if variant else None, offs, lo, df, n_freq,
                      normalize=(variant == 0), want_pgram=True)
-    keep = sizes >= 3  # two observations give exactly degenerate denominators (NaN / inf)
+    # Degenerate objects: two observations give zero denominators (NaN / inf); with
+    # three, the generalized model (mean + cosine + sine) fits exactly, P == 1 at every
+    # frequency and the argmax is rounding noise on both sides.
+    keep = sizes >= (3 if variant == 0 else 5)
     if precision == "plain":
         assert plain_rel_err(r.pgram[keep], ref[keep]) < PLAIN_RTOL
         assert check_best(r.best_idx[keep], ref[keep]) == []
