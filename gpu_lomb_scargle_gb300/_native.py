@@ -17,7 +17,8 @@ DROPIN_LIBS = ("libpylsnoerrorfloat.so", "libpylsnoerrordouble.so", "libpylserro
 # include/lombscargle_py.h).
 LSGB_SYMBOLS = ("lsgb_engine_create", "lsgb_engine_destroy", "lsgb_last_error", "lsgb_version",
                 "lsgb_periodogram_device", "lsgb_periodogram_host", "lsgb_set_tuning",
-                "lsgb_last_launch_info", "lsgb_last_kernel_time")
+                "lsgb_last_launch_info", "lsgb_last_kernel_time", "lsgb_mixed_shapes",
+                "lsgb_get_tuning")
 PYABI_SYMBOLS = ("LombScarglePy", "LombScarglePy_last_status")
 
 
@@ -60,11 +61,15 @@ def lsgb() -> ctypes.CDLL:
         lib.lsgb_periodogram_device.restype = i32
         lib.lsgb_periodogram_host.argtypes = common
         lib.lsgb_periodogram_host.restype = i32
-        lib.lsgb_set_tuning.argtypes = [vp, i32, i32, i32]
+        lib.lsgb_set_tuning.argtypes = [vp, i32, i32, i32, i32, i32]
         lib.lsgb_set_tuning.restype = i32
         lib.lsgb_last_launch_info.argtypes = [vp, c.POINTER(c.c_uint32), c.POINTER(c.c_uint64)]
         lib.lsgb_last_launch_info.restype = i32
         lib.lsgb_last_kernel_time.argtypes = [vp, c.POINTER(c.c_float)]
         lib.lsgb_last_kernel_time.restype = i32
+        lib.lsgb_mixed_shapes.argtypes = [c.POINTER(c.c_int), i32]
+        lib.lsgb_mixed_shapes.restype = i32
+        lib.lsgb_get_tuning.argtypes = [vp, i32, c.POINTER(c.c_int)]
+        lib.lsgb_get_tuning.restype = i32
         lib._lsgb_typed = True
     return lib

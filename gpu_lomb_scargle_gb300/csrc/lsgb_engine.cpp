@@ -86,7 +86,7 @@ struct lsgb_engine {
     cudaStream_t stream = nullptr;  // host-buffer API stream
     DevBuf objs, offs, perm, rec, tile_best, counter;
     DevBuf in_t, in_y, in_dy, out_pg, out_idx, out_p;
-    MixedShape shape[2] = {{16, 256}, {8, 256}};
+    MixedShape shape[2] = {{12, 256, 2, 1}, {8, 256, 2, 1}};
     uint32_t last_kernels = 0;
     uint64_t last_units = 0;
     cudaEvent_t ev_main0 = nullptr, ev_main1 = nullptr;  // around the last main-kernel launch
@@ -139,17 +139,34 @@ LSGB_API void lsgb_engine_destroy(lsgb_engine *eng) {
     delete eng;
 }
 
-LSGB_API int lsgb_set_tuning(lsgb_engine *eng, int variant, int f, int nt) {
+LSGB_API int lsgb_set_tuning(lsgb_engine *eng, int variant, int f, int nt, int minb, int x2) {
     if (!eng || (variant != 0 && variant != 1))
         return fail(LSGB_ERR_INVALID, "lsgb_set_tuning: bad engine or variant");
     MixedShape s = eng->shape[variant];
     if (f > 0) s.f = f;
     if (nt > 0) s.nt = nt;
+    if (minb > 0) s.minb = minb;
+    if (x2 >= 0) s.x2 = x2 ? 1 : 0;
     int blocks = 0;
     if (mixed_occupancy(variant, LSGB_F32, s, 1024, &blocks) != cudaSuccess)
-        return fail(LSGB_ERR_INVALID, "mixed shape F=%d x %d threads is not compiled for variant %d",
-                    s.f, s.nt, variant);
+        return fail(LSGB_ERR_INVALID,
+                    "mixed shape F=%d x %d threads (min %d CTAs/SM, packed %d) is not compiled "
+                    "for variant %d", s.f, s.nt, s.minb, s.x2, variant);
     eng->shape[variant] = s;
+    return LSGB_OK;
+}
+
+LSGB_API int lsgb_mixed_shapes(int *out, int max_shapes) { return mixed_shapes(out, max_shapes); }
+
+LSGB_API int lsgb_get_tuning(lsgb_engine *eng, int variant, int *out5) {
+    if (!eng || !out5 || (variant != 0 && variant != 1))
+        return fail(LSGB_ERR_INVALID, "lsgb_get_tuning: bad argument");
+    const MixedShape s = eng->shape[variant];
+    out5[0] = variant;
+    out5[1] = s.f;
+    out5[2] = s.nt;
+    out5[3] = s.minb;
+    out5[4] = s.x2;
     return LSGB_OK;
 }
 
@@ -249,8 +266,9 @@ LSGB_API int lsgb_periodogram_device(lsgb_engine *eng, int variant, int precisio
         LSGB_CUDA(launch_records(variant, dtype, t, y, dy, (const uint64_t *)eng->offs.p, n_obj,
                                  d_objs, rows, g, (ObsRec *)eng->rec.p, st));
         ++kernels;
-        const uint32_t chunk = std::min<uint32_t>(max_n, kMixedChunkMax);
-        const size_t smem = sizeof(ObsRec) * chunk;
+        const uint32_t rec_bytes = (uint32_t)mixed_rec_bytes(shape);
+        const uint32_t chunk = std::min<uint32_t>(max_n, kMixedSmemMax / rec_bytes);
+        const size_t smem = (size_t)rec_bytes * chunk;
         int occ = 0;
         LSGB_CUDA(mixed_occupancy(variant, dtype, shape, smem, &occ));
         if (occ < 1) return fail(LSGB_ERR_CUDA, "mixed kernel does not fit on an SM (smem %zu)", smem);

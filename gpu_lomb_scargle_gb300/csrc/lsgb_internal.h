@@ -30,6 +30,11 @@ struct ObjInfo {
     double ymean;   // generalized: sum(y/dy^2) / sum(1/dy^2)
     double wsum_f;  // generalized mixed: sum of the stored float weights (~1)
     double ybar_f;  // generalized mixed: sum of the stored float w*y' / wsum_f (~0)
+    // float copies for the mixed kernel, which keeps FP64 out of its loops
+    float norm32;   // (float)norm
+    float invw32;   // (float)(1 / wsum_f)
+    float ybar32;   // (float)ybar_f
+    float pad32;
 };
 
 // Best (power, index) of one (object, frequency tile).
@@ -66,10 +71,14 @@ struct PlainArgs {
     TileBest *tile_best;
 };
 
-// Compiled tile shapes of the mixed kernel (frequencies per thread x threads).
+// Compiled tile shapes of the mixed kernel: frequencies per thread, threads per CTA,
+// and the minimum CTAs per SM its register budget is compiled for.
 struct MixedShape {
-    int f, nt;
+    int f, nt, minb;
+    int x2;  // 1: packed f32x2 loop (two interleaved frequency chains per thread)
 };
+// Bytes of shared memory per staged observation of a mixed shape.
+inline int mixed_rec_bytes(const MixedShape &s) { return s.x2 ? 64 : 32; }
 
 // ---- launchers (lsgb_kernels.cu); all asynchronous on `st` ----
 cudaError_t launch_stats(int variant, int mixed, int dtype, int normalize, const void *y,
@@ -81,6 +90,8 @@ cudaError_t launch_records(int variant, int dtype, const void *t, const void *y,
 cudaError_t launch_mixed(int variant, int dtype, MixedShape shape, const MixedArgs &a,
                          int grid, size_t smem, cudaStream_t st);
 cudaError_t mixed_occupancy(int variant, int dtype, MixedShape shape, size_t smem, int *blocks);
+// Compiled mixed shapes as (variant, F, threads, min CTAs, packed) quintuples; returns the count.
+int mixed_shapes(int *out, int max_shapes);
 cudaError_t launch_plain(int variant, int in_dtype, int out_dtype, const PlainArgs &a, int grid,
                          size_t smem, cudaStream_t st);
 cudaError_t plain_occupancy(int variant, int in_dtype, int out_dtype, size_t smem, int *blocks);
@@ -88,7 +99,7 @@ cudaError_t launch_best_reduce(int dtype, const TileBest *tb, uint32_t n_obj, ui
                                uint32_t *best_idx, void *best_power, cudaStream_t st);
 
 constexpr int kPlainThreads = 256;
-constexpr uint32_t kMixedChunkMax = 2048;  // observations staged in shared memory per pass
+constexpr uint32_t kMixedSmemMax = 64 * 1024;  // shared memory for staged observations per CTA
 constexpr uint32_t kPlainChunkMax = 2048;
 
 }  // namespace lsgb

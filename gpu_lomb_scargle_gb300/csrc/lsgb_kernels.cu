@@ -77,15 +77,16 @@ __device__ __forceinline__ uint64_t frac_turns_u64(double x_hi, double x_lo, dou
 
 // (power, index) ordering of the reference's argmax (source/main.cu:1545-1563):
 // larger power wins, equal power -> lower index (the first maximum).
-__device__ __forceinline__ bool better(double p1, uint32_t k1, double p2, uint32_t k2) {
+template <typename V>
+__device__ __forceinline__ bool better(V p1, uint32_t k1, V p2, uint32_t k2) {
     return p1 > p2 || (p1 == p2 && k1 < k2);
 }
 
-template <int NT>
-__device__ __forceinline__ void block_best(double &bp, uint32_t &bk, double *s_p, uint32_t *s_k) {
+template <int NT, typename V>
+__device__ __forceinline__ void block_best(V &bp, uint32_t &bk, V *s_p, uint32_t *s_k) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        const double op = __shfl_xor_sync(0xffffffffu, bp, o);
+        const V op = __shfl_xor_sync(0xffffffffu, bp, o);
         const uint32_t ok = __shfl_xor_sync(0xffffffffu, bk, o);
         if (better(op, ok, bp, bk)) { bp = op; bk = ok; }
     }
@@ -93,11 +94,11 @@ __device__ __forceinline__ void block_best(double &bp, uint32_t &bk, double *s_p
     if (l == 0) { s_p[w] = bp; s_k[w] = bk; }
     __syncthreads();
     if (w == 0) {
-        bp = l < NT / 32 ? s_p[l] : 0.0;
+        bp = l < NT / 32 ? s_p[l] : V(0);
         bk = l < NT / 32 ? s_k[l] : 0xffffffffu;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-            const double op = __shfl_xor_sync(0xffffffffu, bp, o);
+            const V op = __shfl_xor_sync(0xffffffffu, bp, o);
             const uint32_t ok = __shfl_xor_sync(0xffffffffu, bk, o);
             if (better(op, ok, bp, bk)) { bp = op; bk = ok; }
         }
@@ -131,11 +132,15 @@ __global__ void stats_kernel(int variant, int mixed, int dtype, int normalize, c
         if (threadIdx.x == 0) {
             const double sigma = sqrt(s2 / (n * 1.0));
             ob.norm = normalize ? 2.0 / (n * (sigma * sigma)) : 1.0;
+            ob.norm32 = (float)ob.norm;
         }
         return;
     }
     if (!mixed) {
-        if (threadIdx.x == 0) ob.norm = 1.0;
+        if (threadIdx.x == 0) {
+            ob.norm = 1.0;
+            ob.norm32 = 1.0f;
+        }
         return;
     }
     double w_s = 0.0, wy_s = 0.0;
@@ -167,6 +172,9 @@ __global__ void stats_kernel(int variant, int mixed, int dtype, int normalize, c
         ob.ybar_f = yf / wf;
         const double ybar = yf / wf;
         ob.norm = 1.0 / (yy - ybar * ybar);
+        ob.norm32 = (float)ob.norm;
+        ob.invw32 = (float)(1.0 / wf);
+        ob.ybar32 = (float)ybar;
     }
 }
 
@@ -270,12 +278,45 @@ __device__ __forceinline__ void store_out_d(void *pgram, uint64_t i, double p) {
     reinterpret_cast<OutT *>(pgram)[i] = (OutT)p;
 }
 
-template <int F, int NT, bool GEN, typename OutT>
-__global__ void __launch_bounds__(NT, 2) mixed_kernel(MixedArgs a) {
+// Packed FP32 pairs (Blackwell f32x2): one instruction issues two FP32 lanes' work.
+__device__ __forceinline__ uint64_t ffma2(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ uint64_t fmul2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t fadd2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t pack2(float lo, float hi) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void unpack2(uint64_t v, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+
+// Shared-memory record of the packed (X2) loop, expanded from ObsRec at staging:
+//   q0 = {a_lo, a_hi, b_lo, b_hi}
+//   q1 = {v0, v0, cd, sd}            ({y,y} or {w,w}; the single step for the odd chain)
+//   q2 = {cd2, cd2, sd2, sd2}        (the double step of both chains)
+//   q3 = {-sd2, -sd2, v1, v1}        ({wy, wy} for the generalized variant)
+// Each 64-bit half of q1..q3 is a ready-made packed operand.
+constexpr int kX2RecBytes = 64;
+
+template <int F, int NT, int MINB, bool GEN, bool X2, typename OutT>
+__global__ void __launch_bounds__(NT, MINB) mixed_kernel(MixedArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     uint4 *s_rec = reinterpret_cast<uint4 *>(smem_raw);  // 2 x uint4 per observation
     __shared__ uint32_t s_unit;
-    __shared__ double s_bp[NT / 32];
+    __shared__ float s_bp[NT / 32];
     __shared__ uint32_t s_bk[NT / 32];
     constexpr int NA = GEN ? 6 : 4;
     const uint32_t units = a.n_obj * a.n_tiles;
@@ -291,73 +332,139 @@ __global__ void __launch_bounds__(NT, 2) mixed_kernel(MixedArgs a) {
         const uint32_t n = a.objs[o].n;
         const uint32_t k0 = tile * (uint32_t)(NT * F) + threadIdx.x * (uint32_t)F;
 
+        // X2: two interleaved chains (even / odd frequencies of the run) advance by 2 steps
+        // as packed pairs; accumulator pair p holds frequencies (k0+2p, k0+2p+1).
+        static_assert(!X2 || F % 2 == 0, "the packed loop needs an even F");
+        constexpr int NP = X2 ? F / 2 : 1;
         float acc[NA][F];
+        uint64_t acc2[NA][NP];
 #pragma unroll
-        for (int q = 0; q < NA; ++q)
+        for (int q = 0; q < NA; ++q) {
 #pragma unroll
             for (int f = 0; f < F; ++f) acc[q][f] = 0.0f;
+#pragma unroll
+            for (int p = 0; p < NP; ++p) acc2[q][p] = 0ull;
+        }
 
         for (uint32_t c0 = 0; c0 < n; c0 += a.chunk) {
             const uint32_t cnt = min(a.chunk, n - c0);
             const uint4 *src = reinterpret_cast<const uint4 *>(a.rec + row0 + c0);
-            for (uint32_t i = threadIdx.x; i < 2 * cnt; i += NT) s_rec[i] = __ldg(src + i);
+            if (!X2) {
+                for (uint32_t i = threadIdx.x; i < 2 * cnt; i += NT) s_rec[i] = __ldg(src + i);
+            } else {
+                for (uint32_t i = threadIdx.x; i < cnt; i += NT) {
+                    const uint4 q0 = __ldg(src + 2 * i);
+                    const uint4 qv = __ldg(src + 2 * i + 1);
+                    const float v0 = __uint_as_float(qv.x), v1 = __uint_as_float(qv.y);
+                    const float cd = __uint_as_float(qv.z), sd = __uint_as_float(qv.w);
+                    const float cd2 = fmaf(cd, cd, -sd * sd), sd2 = 2.0f * cd * sd;
+                    float4 *d = reinterpret_cast<float4 *>(s_rec) + 4 * i;
+                    reinterpret_cast<uint4 *>(d)[0] = q0;
+                    d[1] = make_float4(v0, v0, cd, sd);
+                    d[2] = make_float4(cd2, cd2, sd2, sd2);
+                    d[3] = make_float4(-sd2, -sd2, v1, v1);
+                }
+            }
             __syncthreads();
 #pragma unroll 1
             for (uint32_t j = 0; j < cnt; ++j) {
-                const uint4 ab = s_rec[2 * j];
-                const float4 v = reinterpret_cast<const float4 *>(s_rec)[2 * j + 1];
+                const uint4 ab = X2 ? s_rec[4 * j] : s_rec[2 * j];
                 // anchor: top 32 bits of a + k0*b (mod 2^64), as a signed turn count
                 const uint64_t p = (uint64_t)k0 * ab.z + (((uint64_t)ab.y << 32) | ab.x);
                 const uint32_t hi = (uint32_t)(p >> 32) + k0 * ab.w;
                 float s, c;
                 __sincosf((float)(int32_t)hi * kTwoPiOver2p32f, &s, &c);
+                if (!X2) {
+                    const float4 v = reinterpret_cast<const float4 *>(s_rec)[2 * j + 1];
 #pragma unroll
-                for (int f = 0; f < F; ++f) {
-                    if (!GEN) {
-                        acc[0][f] = fmaf(v.x, c, acc[0][f]);  // XC
-                        acc[1][f] = fmaf(v.x, s, acc[1][f]);  // XS
-                        acc[2][f] = fmaf(c, c, acc[2][f]);    // CC
-                        acc[3][f] = fmaf(c, s, acc[3][f]);    // CS
-                    } else {
-                        const float wc = v.x * c;
-                        acc[0][f] += wc;                       // C
-                        acc[1][f] = fmaf(v.x, s, acc[1][f]);   // S
-                        acc[2][f] = fmaf(v.y, c, acc[2][f]);   // YC
-                        acc[3][f] = fmaf(v.y, s, acc[3][f]);   // YS
-                        acc[4][f] = fmaf(wc, c, acc[4][f]);    // CC
-                        acc[5][f] = fmaf(wc, s, acc[5][f]);    // CS
+                    for (int f = 0; f < F; ++f) {
+                        if (!GEN) {
+                            acc[0][f] = fmaf(v.x, c, acc[0][f]);  // XC
+                            acc[1][f] = fmaf(v.x, s, acc[1][f]);  // XS
+                            acc[2][f] = fmaf(c, c, acc[2][f]);    // CC
+                            acc[3][f] = fmaf(c, s, acc[3][f]);    // CS
+                        } else {
+                            const float wc = v.x * c;
+                            acc[0][f] += wc;                       // C
+                            acc[1][f] = fmaf(v.x, s, acc[1][f]);   // S
+                            acc[2][f] = fmaf(v.y, c, acc[2][f]);   // YC
+                            acc[3][f] = fmaf(v.y, s, acc[3][f]);   // YS
+                            acc[4][f] = fmaf(wc, c, acc[4][f]);    // CC
+                            acc[5][f] = fmaf(wc, s, acc[5][f]);    // CS
+                        }
+                        if (f + 1 < F) {
+                            const float cn = fmaf(c, v.z, -s * v.w);
+                            s = fmaf(s, v.z, c * v.w);
+                            c = cn;
+                        }
                     }
-                    if (f + 1 < F) {
-                        const float cn = fmaf(c, v.z, -s * v.w);
-                        s = fmaf(s, v.z, c * v.w);
-                        c = cn;
+                } else {
+                    const ulonglong2 q1 = reinterpret_cast<const ulonglong2 *>(s_rec)[4 * j + 1];
+                    const ulonglong2 q2 = reinterpret_cast<const ulonglong2 *>(s_rec)[4 * j + 2];
+                    const ulonglong2 q3 = reinterpret_cast<const ulonglong2 *>(s_rec)[4 * j + 3];
+                    float cd, sd;
+                    unpack2(q1.y, cd, sd);
+                    const float c1 = fmaf(c, cd, -s * sd);  // odd chain: one step ahead
+                    const float s1 = fmaf(s, cd, c * sd);
+                    uint64_t C = pack2(c, c1), S = pack2(s, s1);
+                    const uint64_t V0 = q1.x, CD2 = q2.x, SD2 = q2.y, NSD2 = q3.x, V1 = q3.y;
+#pragma unroll
+                    for (int pp = 0; pp < NP; ++pp) {
+                        if (!GEN) {
+                            acc2[0][pp] = ffma2(V0, C, acc2[0][pp]);  // XC
+                            acc2[1][pp] = ffma2(V0, S, acc2[1][pp]);  // XS
+                            acc2[2][pp] = ffma2(C, C, acc2[2][pp]);   // CC
+                            acc2[3][pp] = ffma2(C, S, acc2[3][pp]);   // CS
+                        } else {
+                            const uint64_t WC = fmul2(V0, C);
+                            acc2[0][pp] = fadd2(acc2[0][pp], WC);     // C
+                            acc2[1][pp] = ffma2(V0, S, acc2[1][pp]);  // S
+                            acc2[2][pp] = ffma2(V1, C, acc2[2][pp]);  // YC
+                            acc2[3][pp] = ffma2(V1, S, acc2[3][pp]);  // YS
+                            acc2[4][pp] = ffma2(WC, C, acc2[4][pp]);  // CC
+                            acc2[5][pp] = ffma2(WC, S, acc2[5][pp]);  // CS
+                        }
+                        if (pp + 1 < NP) {
+                            const uint64_t t1 = fmul2(S, NSD2);
+                            const uint64_t t2 = fmul2(C, SD2);
+                            C = ffma2(C, CD2, t1);
+                            S = ffma2(S, CD2, t2);
+                        }
                     }
                 }
             }
             __syncthreads();
         }
+        if (X2) {
+#pragma unroll
+            for (int q = 0; q < NA; ++q)
+#pragma unroll
+                for (int pp = 0; pp < NP; ++pp) {
+                    unpack2(acc2[q][pp], acc[q][2 * pp], acc[q][2 * pp + 1]);
+                }
+        }
 
-        // epilogue: power, optional store, thread-local first maximum
-        double bp = 0.0;
+        // epilogue: power, optional store, thread-local first maximum (all FP32: the
+        // FP64 pipe of this part is 1/64 of the FP32 rate)
+        float bp = 0.0f;
         uint32_t bk = 0xffffffffu;
         if (tile == 0 && threadIdx.x == 0) bk = 0;  // the reference's (power 0, index 0) start
         const uint64_t out0 = (uint64_t)o * a.n_freq;
+        const float nrm = a.objs[o].norm32;
         if (!GEN) {
             const float N = (float)n;
-            const float nrm = (float)a.objs[o].norm;
 #pragma unroll
             for (int f = 0; f < F; ++f) {
                 const uint32_t k = k0 + f;
                 const float P = std_power_f(N, acc[0][f], acc[1][f], acc[2][f], acc[3][f]) * nrm;
                 if (k < a.n_freq) {
                     if (a.pgram) store_out<OutT>(a.pgram, out0 + k, P);
-                    if ((double)P > bp) { bp = (double)P; bk = k; }
+                    if (P > bp) { bp = P; bk = k; }
                 }
             }
         } else {
-            const float invW = (float)(1.0 / a.objs[o].wsum_f);
-            const float ybar = (float)a.objs[o].ybar_f;
-            const float nrm = (float)a.objs[o].norm;
+            const float invW = a.objs[o].invw32;
+            const float ybar = a.objs[o].ybar32;
 #pragma unroll
             for (int f = 0; f < F; ++f) {
                 const uint32_t k = k0 + f;
@@ -365,15 +472,15 @@ __global__ void __launch_bounds__(NT, 2) mixed_kernel(MixedArgs a) {
                                             acc[4][f], acc[5][f]) * nrm;
                 if (k < a.n_freq) {
                     if (a.pgram) store_out<OutT>(a.pgram, out0 + k, P);
-                    if ((double)P > bp) { bp = (double)P; bk = k; }
+                    if (P > bp) { bp = P; bk = k; }
                 }
             }
         }
         if (a.tile_best) {
-            block_best<NT>(bp, bk, s_bp, s_bk);
+            block_best<NT, float>(bp, bk, s_bp, s_bk);
             if (threadIdx.x == 0) {
                 TileBest tb;
-                tb.p = bp;
+                tb.p = (double)bp;
                 tb.k = bk;
                 tb.pad = 0;
                 a.tile_best[(uint64_t)o * a.n_tiles + tile] = tb;
@@ -533,7 +640,7 @@ __global__ void __launch_bounds__(NT) plain_kernel(PlainArgs a) {
             if (Pr > bp) { bp = Pr; bk = k; }
         }
         if (a.tile_best) {
-            block_best<NT>(bp, bk, s_bp, s_bk);
+            block_best<NT, double>(bp, bk, s_bp, s_bk);
             if (threadIdx.x == 0) {
                 TileBest tb;
                 tb.p = bp;
@@ -574,15 +681,15 @@ __global__ void best_reduce_kernel(const TileBest *tb, uint32_t n_obj, uint32_t 
     }
 }
 
-template <int F, int NT, bool GEN>
+template <int F, int NT, int MINB, bool GEN, bool X2>
 cudaError_t launch_mixed_t(int dtype, const MixedArgs &a, int grid, size_t smem, cudaStream_t st) {
     if (dtype == 0) {
-        auto k = mixed_kernel<F, NT, GEN, float>;
+        auto k = mixed_kernel<F, NT, MINB, GEN, X2, float>;
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         k<<<grid, NT, smem, st>>>(a);
     } else {
-        auto k = mixed_kernel<F, NT, GEN, double>;
+        auto k = mixed_kernel<F, NT, MINB, GEN, X2, double>;
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         k<<<grid, NT, smem, st>>>(a);
@@ -590,30 +697,35 @@ cudaError_t launch_mixed_t(int dtype, const MixedArgs &a, int grid, size_t smem,
     return cudaGetLastError();
 }
 
-template <int F, int NT, bool GEN>
+template <int F, int NT, int MINB, bool GEN, bool X2>
 cudaError_t occ_mixed_t(int dtype, size_t smem, int *blocks) {
     cudaError_t e;
     if (dtype == 0) {
-        auto k = mixed_kernel<F, NT, GEN, float>;
+        auto k = mixed_kernel<F, NT, MINB, GEN, X2, float>;
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k, NT, smem);
     } else {
-        auto k = mixed_kernel<F, NT, GEN, double>;
+        auto k = mixed_kernel<F, NT, MINB, GEN, X2, double>;
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k, NT, smem);
     }
     return e;
 }
 
-// The compiled mixed shapes. Keep in sync with kMixedShapes in lsgb_engine.cu.
-#define LSGB_MIXED_SHAPES(X) \
-    X(16, 256, false)        \
-    X(8, 256, false)         \
-    X(8, 128, false)         \
-    X(4, 256, false)         \
-    X(8, 256, true)          \
-    X(4, 256, true)          \
-    X(12, 256, true)
+// The compiled mixed shapes: (frequencies per thread, threads, min CTAs per SM for
+// the register budget, generalized?, packed f32x2 loop?).
+#define LSGB_MIXED_SHAPES(X)    \
+    X(16, 256, 2, false, false) \
+    X(16, 128, 4, false, false) \
+    X(8, 256, 3, false, false)  \
+    X(16, 256, 2, false, true)  \
+    X(16, 128, 4, false, true)  \
+    X(12, 256, 2, false, true)  \
+    X(8, 256, 3, false, true)   \
+    X(12, 256, 2, true, false)  \
+    X(6, 256, 3, true, false)   \
+    X(12, 256, 2, true, true)   \
+    X(8, 256, 2, true, true)
 
 }  // namespace
 
@@ -637,18 +749,36 @@ cudaError_t launch_records(int variant, int dtype, const void *t, const void *y,
 
 cudaError_t launch_mixed(int variant, int dtype, MixedShape shape, const MixedArgs &a, int grid,
                          size_t smem, cudaStream_t st) {
-#define X(F_, NT_, G_)                                                   \
-    if (shape.f == F_ && shape.nt == NT_ && (variant == 1) == G_)        \
-        return launch_mixed_t<F_, NT_, G_>(dtype, a, grid, smem, st);
+#define X(F_, NT_, MB_, G_, X2_)                                                    \
+    if (shape.f == F_ && shape.nt == NT_ && shape.minb == MB_ && (variant == 1) == G_ && \
+        (shape.x2 != 0) == X2_)                                                          \
+        return launch_mixed_t<F_, NT_, MB_, G_, X2_>(dtype, a, grid, smem, st);
     LSGB_MIXED_SHAPES(X)
 #undef X
     return cudaErrorInvalidValue;
 }
 
+int mixed_shapes(int *out, int max_shapes) {
+    int n = 0;
+#define X(F_, NT_, MB_, G_, X2_)                 \
+    if (out && n < max_shapes) {                 \
+        out[5 * n + 0] = G_ ? 1 : 0;             \
+        out[5 * n + 1] = F_;                     \
+        out[5 * n + 2] = NT_;                    \
+        out[5 * n + 3] = MB_;                    \
+        out[5 * n + 4] = X2_ ? 1 : 0;            \
+    }                                            \
+    ++n;
+    LSGB_MIXED_SHAPES(X)
+#undef X
+    return n;
+}
+
 cudaError_t mixed_occupancy(int variant, int dtype, MixedShape shape, size_t smem, int *blocks) {
-#define X(F_, NT_, G_)                                            \
-    if (shape.f == F_ && shape.nt == NT_ && (variant == 1) == G_) \
-        return occ_mixed_t<F_, NT_, G_>(dtype, smem, blocks);
+#define X(F_, NT_, MB_, G_, X2_)                                                    \
+    if (shape.f == F_ && shape.nt == NT_ && shape.minb == MB_ && (variant == 1) == G_ && \
+        (shape.x2 != 0) == X2_)                                                          \
+        return occ_mixed_t<F_, NT_, MB_, G_, X2_>(dtype, smem, blocks);
     LSGB_MIXED_SHAPES(X)
 #undef X
     return cudaErrorInvalidValue;

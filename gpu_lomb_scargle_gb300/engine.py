@@ -81,8 +81,15 @@ class Engine:
         except Exception:
             pass
 
-    def set_tuning(self, variant: int, freqs_per_thread: int = 0, threads: int = 0):
-        self._check(self._lib.lsgb_set_tuning(self._h, variant, freqs_per_thread, threads))
+    def set_tuning(self, variant: int, freqs_per_thread: int = 0, threads: int = 0,
+                   min_ctas: int = 0, packed: int = -1):
+        self._check(self._lib.lsgb_set_tuning(self._h, variant, freqs_per_thread, threads,
+                                              min_ctas, packed))
+
+    def get_tuning(self, variant: int):
+        out = (ctypes.c_int * 5)()
+        self._check(self._lib.lsgb_get_tuning(self._h, variant, out))
+        return tuple(out)[1:]
 
     def launch_info(self):
         k = ctypes.c_uint32()
@@ -139,6 +146,15 @@ class Engine:
             int(n_freq), int(bool(normalize)), vp(pg), vp(idx), vp(pw))
         self._check(rc)
         return Result(idx, pw, pg)
+
+
+def mixed_shapes():
+    """Compiled mixed-kernel shapes: list of (variant, F, threads, min_ctas, packed)."""
+    lib = _native.lsgb()
+    n = lib.lsgb_mixed_shapes(None, 0)
+    buf = (ctypes.c_int * (5 * n))()
+    lib.lsgb_mixed_shapes(buf, n)
+    return [tuple(buf[5 * i:5 * i + 5]) for i in range(n)]
 
 
 _default: Engine | None = None

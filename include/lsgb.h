@@ -88,11 +88,19 @@ LSGB_API int lsgb_periodogram_host(lsgb_engine *eng, int variant, int precision,
                                    uint32_t n_freq, int normalize, void *pgram, uint32_t *best_idx,
                                    void *best_power);
 
-/* Tuning of the mixed kernel: frequencies per thread (F) and threads per CTA.
- * 0 keeps the built-in choice. Returns LSGB_ERR_INVALID for shapes that are not
- * compiled in. */
+/* Tuning of the mixed kernel: frequencies per thread (F), threads per CTA, the
+ * minimum CTAs per SM the kernel's register budget is compiled for, and the packed
+ * f32x2 inner loop (1) or the scalar one (0). 0 (-1 for packed) keeps the current
+ * value. Returns LSGB_ERR_INVALID for shapes that are not compiled in. */
 LSGB_API int lsgb_set_tuning(lsgb_engine *eng, int variant, int freqs_per_thread,
-                             int threads_per_cta);
+                             int threads_per_cta, int min_ctas_per_sm, int packed);
+
+/* The compiled mixed-kernel shapes, as out[5*i .. 5*i+4] = (variant, F, threads,
+ * min CTAs per SM, packed), at most max_shapes of them. Returns how many exist. */
+LSGB_API int lsgb_mixed_shapes(int *out, int max_shapes);
+
+/* The shape the engine uses for a variant, in the same 5-int layout. */
+LSGB_API int lsgb_get_tuning(lsgb_engine *eng, int variant, int *out5);
 
 /* Launch statistics of the last call: kernels launched and the work units the
  * persistent kernel processed. */

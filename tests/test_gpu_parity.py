@@ -189,3 +189,40 @@ def test_device_api_matches_host_api(eng):
     assert np.array_equal(bi.cpu().numpy().astype(np.uint32), h.best_idx)
     k, units = eng.launch_info()
     assert k >= 3 and units > 0
+
+
+def _compiled_shapes():
+    try:
+        return E.mixed_shapes()
+    except Exception:  # library not built yet: nothing to parametrize (collected as skipped)
+        return []
+
+
+@pytest.mark.parametrize("shape", _compiled_shapes(), ids=lambda s: "v%d_F%d_nt%d_mb%d_x%d" % s)
+def test_every_compiled_mixed_shape(eng, shape):
+    """Each compiled (F, threads, min CTAs, packed) shape of the mixed kernel against the
+    oracle, on a batch whose objects span several staging chunks and partial tiles."""
+    variant = shape[0]
+    w = synth.lognormal_batch(seed=300 + variant, n_obj=16, n_freq=9001, error=bool(variant))
+    # add one long object (more observations than one shared-memory chunk holds)
+    rng = np.random.default_rng(7)
+    n_long = 2500
+    t_long = np.sort(rng.uniform(0, 1800, n_long))
+    y_long = np.sin(TWO_PI * t_long / 1.3) + rng.normal(0, 0.5, n_long)
+    t = np.concatenate([w.t, t_long])
+    y = np.concatenate([w.y, y_long])
+    dy = np.concatenate([w.dy, rng.uniform(0.01, 0.1, n_long) if variant else np.ones(n_long)])
+    offs = np.concatenate([w.offsets, [w.offsets[-1] + n_long]]).astype(np.uint64)
+    if variant == 1:
+        _, y = pyoracle.batch_pgram(1, t, y, dy, offs, w.fmin, w.df, n_freq=1)
+    ref, _ = pyoracle.batch_pgram(variant, t, y, dy, offs, w.fmin, w.df, n_freq=w.n_freq)
+    saved = eng.get_tuning(variant)
+    try:
+        eng.set_tuning(variant, *shape[1:])
+        r = eng.run_host(variant, "mixed", t, y, dy if variant else None, offs, w.fmin, w.df,
+                         w.n_freq, normalize=(variant == 0), want_pgram=True)
+    finally:
+        eng.set_tuning(variant, *saved)
+    err = mixed_abs_err(r.pgram, ref)
+    assert err < MIXED_ATOL, err
+    assert check_best(r.best_idx, ref, tol=MIXED_ATOL) == []
