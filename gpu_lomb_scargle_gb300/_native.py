@@ -18,7 +18,7 @@ DROPIN_LIBS = ("libpylsnoerrorfloat.so", "libpylsnoerrordouble.so", "libpylserro
 LSGB_SYMBOLS = ("lsgb_engine_create", "lsgb_engine_destroy", "lsgb_last_error", "lsgb_version",
                 "lsgb_periodogram_device", "lsgb_periodogram_host", "lsgb_set_tuning",
                 "lsgb_last_launch_info", "lsgb_last_kernel_time", "lsgb_mixed_shapes",
-                "lsgb_get_tuning")
+                "lsgb_get_tuning", "lsgb_periodogram_noalloc")
 PYABI_SYMBOLS = ("LombScarglePy", "LombScarglePy_last_status")
 
 
@@ -71,5 +71,8 @@ def lsgb() -> ctypes.CDLL:
         lib.lsgb_mixed_shapes.restype = i32
         lib.lsgb_get_tuning.argtypes = [vp, i32, c.POINTER(c.c_int)]
         lib.lsgb_get_tuning.restype = i32
+        lib.lsgb_periodogram_noalloc.argtypes = [i32, i32, vp, vp, vp, u64p, u32, dbl, dbl, u32,
+                                                 i32, vp, vp, vp, vp]
+        lib.lsgb_periodogram_noalloc.restype = i32
         lib._lsgb_typed = True
     return lib

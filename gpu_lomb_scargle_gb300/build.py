@@ -77,6 +77,9 @@ def build(force: bool = False, jobs: int = 0, verbose: bool = False) -> Path:
     compile_steps.append(([nv, *ARCH, *NVCC_COMMON, "-Xptxas", "-v", "-c",
                            str(CSRC / "lsgb_kernels.cu"), "-o", str(k_obj)],
                           k_obj, [CSRC / "lsgb_kernels.cu", *HEADERS]))
+    n_obj = OBJ / "lsgb_noalloc.o"
+    compile_steps.append(([nv, *ARCH, *NVCC_COMMON, "-c", str(CSRC / "lsgb_noalloc.cu"), "-o",
+                           str(n_obj)], n_obj, [CSRC / "lsgb_noalloc.cu", *HEADERS]))
     e_obj = OBJ / "lsgb_engine.o"
     compile_steps.append(([nv, *NVCC_COMMON, *HOST_FLAGS, "-c", str(CSRC / "lsgb_engine.cpp"),
                            "-o", str(e_obj)], e_obj, [CSRC / "lsgb_engine.cpp", *HEADERS]))
@@ -94,8 +97,8 @@ def build(force: bool = False, jobs: int = 0, verbose: bool = False) -> Path:
             if verbose and log and log != "cached":
                 print(f"[{out.name}]\n{log}")
     link = [nv, *ARCH, "-shared", "-cudart", "shared", "-Xcompiler", "-fopenmp"]
-    link_steps = [(link + [str(k_obj), str(e_obj), "-o", str(LIB / "liblsgb.so")],
-                   LIB / "liblsgb.so", [k_obj, e_obj])]
+    link_steps = [(link + [str(k_obj), str(e_obj), str(n_obj), "-o", str(LIB / "liblsgb.so")],
+                   LIB / "liblsgb.so", [k_obj, e_obj, n_obj])]
     for lib, o in v_objs.items():
         link_steps.append((link + [str(o), str(k_obj), str(e_obj), "-o", str(LIB / lib)],
                            LIB / lib, [o, k_obj, e_obj]))

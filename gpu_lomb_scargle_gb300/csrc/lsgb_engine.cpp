@@ -80,6 +80,11 @@ void two_prod(double a, double b_hi, double b_lo, double &hi, double &lo) {
 
 }  // namespace
 
+namespace lsgb {
+// Lets other translation units of the library report through lsgb_last_error().
+void set_last_error(const char *msg) { g_last_error = msg; }
+}  // namespace lsgb
+
 struct lsgb_engine {
     int device = 0;
     int sms = 0;

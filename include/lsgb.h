@@ -95,6 +95,34 @@ LSGB_API int lsgb_periodogram_host(lsgb_engine *eng, int variant, int precision,
 LSGB_API int lsgb_set_tuning(lsgb_engine *eng, int variant, int freqs_per_thread,
                              int threads_per_cta, int min_ctas_per_sm, int packed);
 
+/* The mixed-form periodogram of lsgb_periodogram_device, with no allocation at all.
+ * No counterpart in the reference.
+ *
+ * For callers that must not allocate device memory while they run: a plugin inside
+ * a framework whose own allocator owns the device-memory budget, a latency-critical
+ * loop that cannot take the synchronization cudaMalloc/cudaFree may cause, or a
+ * service that reserves its whole footprint at start-up. The regular entry points
+ * grow engine buffers with cudaMalloc; this one needs no engine and uses one
+ * fixed-size scratch array compiled into liblsgb.so (about 8.3 MiB, held on every
+ * GPU that loads the library until the process exits).
+ *
+ * Arguments as lsgb_periodogram_device (mixed form; t, y, dy, pgram, best_idx and
+ * best_power are caller-owned device memory; offsets is host memory). Limits of one
+ * call: at most 131072 observations, 2048 objects, and 262144 (object x frequency
+ * tile) units, a tile being 3072 frequencies for LSGB_STANDARD and 2048 for
+ * LSGB_GENERALIZED; larger calls return LSGB_ERR_INVALID with the limit in
+ * lsgb_last_error(). The first call on each device looks up the scratch array's
+ * device address on that device (make that first call before any stream capture).
+ * All calls share the one array and leave its contents behind, so calls whose GPU
+ * work overlaps (different streams or host threads without ordering) race; order
+ * them. Host set-up is serialized internally and waits for the stream's earlier
+ * work before launching. */
+LSGB_API int lsgb_periodogram_noalloc(int variant, int dtype, const void *t, const void *y,
+                                      const void *dy, const uint64_t *offsets_host,
+                                      uint32_t n_obj, double fmin, double df, uint32_t n_freq,
+                                      int normalize, void *pgram, uint32_t *best_idx,
+                                      void *best_power, void *stream);
+
 /* The compiled mixed-kernel shapes, as out[5*i .. 5*i+4] = (variant, F, threads,
  * min CTAs per SM, packed), at most max_shapes of them. Returns how many exist. */
 LSGB_API int lsgb_mixed_shapes(int *out, int max_shapes);
