@@ -222,6 +222,8 @@ def main():
     ap.add_argument("--ref-freqs", type=int, default=2_000,
                     help="frequencies per step of the reference arm")
     ap.add_argument("--no-dropin", action="store_true")
+    ap.add_argument("--serve-objects", type=int, default=100_000,
+                    help="objects of the Poisson serving replay (0 = skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -368,6 +370,18 @@ def main():
                                "d2h_bytes_per_step": int(pg.nbytes),
                                "api": "LombScarglePy, libpylsnoerrorfloat.so, MODE 1, full pgram"}
         del pg
+
+    if args.serve_objects:
+        from gpu_lomb_scargle_gb300 import serve
+        eng.close()
+        torch.cuda.empty_cache()
+        st = synth.stream(n_obj=args.serve_objects)
+        rep, _ = serve.replay(st, slots=3, max_batch=4096, hbm_budget_bytes=4 << 30)
+        rep["workload"] = (f"{st.size.size} objects, Poisson {2000} objects/s, sizes "
+                           "round(LogNormal(ln 80, 0.8)) in [10, 1000], 2e5 frequencies, mixed form")
+        extra["serving"] = rep
+        extra["p50_latency_ms"] = rep["latency_p50_ms"]
+        extra["p99_latency_ms"] = rep["latency_p99_ms"]
 
     cpu = cpu_baseline(w, args.cpu_freqs) if args.cpu_freqs else None
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -18,7 +18,9 @@ DROPIN_LIBS = ("libpylsnoerrorfloat.so", "libpylsnoerrordouble.so", "libpylserro
 LSGB_SYMBOLS = ("lsgb_engine_create", "lsgb_engine_destroy", "lsgb_last_error", "lsgb_version",
                 "lsgb_periodogram_device", "lsgb_periodogram_host", "lsgb_set_tuning",
                 "lsgb_last_launch_info", "lsgb_last_kernel_time", "lsgb_mixed_shapes",
-                "lsgb_get_tuning", "lsgb_periodogram_noalloc")
+                "lsgb_get_tuning", "lsgb_periodogram_noalloc", "lsgb_server_create",
+                "lsgb_server_submit", "lsgb_server_poll", "lsgb_server_stats", "lsgb_server_now",
+                "lsgb_server_destroy", "lsgb_set_reanchor")
 PYABI_SYMBOLS = ("LombScarglePy", "LombScarglePy_last_status")
 
 
@@ -74,5 +76,20 @@ def lsgb() -> ctypes.CDLL:
         lib.lsgb_periodogram_noalloc.argtypes = [i32, i32, vp, vp, vp, u64p, u32, dbl, dbl, u32,
                                                  i32, vp, vp, vp, vp]
         lib.lsgb_periodogram_noalloc.restype = i32
+        dp = c.POINTER(c.c_double)
+        lib.lsgb_server_create.argtypes = [i32, i32, i32, dbl, dbl, u32, i32, u32, u32, c.c_uint64,
+                                           c.POINTER(vp)]
+        lib.lsgb_server_create.restype = i32
+        lib.lsgb_server_submit.argtypes = [vp, c.c_uint64, dp, dp, dp, u32]
+        lib.lsgb_server_submit.restype = i32
+        lib.lsgb_server_poll.argtypes = [vp, u32, u64p, c.POINTER(c.c_uint32), dp, dp, dp]
+        lib.lsgb_server_poll.restype = i32
+        lib.lsgb_server_stats.argtypes = [vp, u64p]
+        lib.lsgb_server_stats.restype = i32
+        lib.lsgb_server_now.restype = dbl
+        lib.lsgb_server_destroy.argtypes = [vp]
+        lib.lsgb_server_destroy.restype = None
+        lib.lsgb_set_reanchor.argtypes = [vp, u32]
+        lib.lsgb_set_reanchor.restype = i32
         lib._lsgb_typed = True
     return lib

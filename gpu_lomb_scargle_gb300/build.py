@@ -5,7 +5,8 @@ Outputs, in ``gpu_lomb_scargle_gb300/lib/``:
 * ``liblsgb.so``                -- the engine and its ``lsgb_*`` C ABI (include/lsgb.h);
 * ``libpyls{noerror,error}{float,double}.so`` -- the four drop-in libraries exporting
   ``LombScarglePy`` (include/lombscargle_py.h), the file names
-  source/lombscarglegpu.py:279-287 loads.
+  source/lombscarglegpu.py:279-287 loads;
+* ``lsgb_main`` -- the command-line front end (the reference's paper and release CLIs).
 
 Device code is compiled once, for sm_103a only, and linked into every library.
 Objects are rebuilt only when a source or header is newer than them.
@@ -80,6 +81,9 @@ def build(force: bool = False, jobs: int = 0, verbose: bool = False) -> Path:
     n_obj = OBJ / "lsgb_noalloc.o"
     compile_steps.append(([nv, *ARCH, *NVCC_COMMON, "-c", str(CSRC / "lsgb_noalloc.cu"), "-o",
                            str(n_obj)], n_obj, [CSRC / "lsgb_noalloc.cu", *HEADERS]))
+    s_obj = OBJ / "lsgb_server.o"
+    compile_steps.append(([nv, *NVCC_COMMON, *HOST_FLAGS, "-c", str(CSRC / "lsgb_server.cpp"),
+                           "-o", str(s_obj)], s_obj, [CSRC / "lsgb_server.cpp", *HEADERS]))
     e_obj = OBJ / "lsgb_engine.o"
     compile_steps.append(([nv, *NVCC_COMMON, *HOST_FLAGS, "-c", str(CSRC / "lsgb_engine.cpp"),
                            "-o", str(e_obj)], e_obj, [CSRC / "lsgb_engine.cpp", *HEADERS]))
@@ -97,11 +101,15 @@ def build(force: bool = False, jobs: int = 0, verbose: bool = False) -> Path:
             if verbose and log and log != "cached":
                 print(f"[{out.name}]\n{log}")
     link = [nv, *ARCH, "-shared", "-cudart", "shared", "-Xcompiler", "-fopenmp"]
-    link_steps = [(link + [str(k_obj), str(e_obj), str(n_obj), "-o", str(LIB / "liblsgb.so")],
-                   LIB / "liblsgb.so", [k_obj, e_obj, n_obj])]
+    link_steps = [(link + [str(k_obj), str(e_obj), str(n_obj), str(s_obj), "-o",
+                           str(LIB / "liblsgb.so"), "-lpthread"],
+                   LIB / "liblsgb.so", [k_obj, e_obj, n_obj, s_obj])]
     for lib, o in v_objs.items():
         link_steps.append((link + [str(o), str(k_obj), str(e_obj), "-o", str(LIB / lib)],
                            LIB / lib, [o, k_obj, e_obj]))
+    cli = LIB / "lsgb_main"
+    link_steps.append(([nv, *NVCC_COMMON, "-O2", str(CSRC / "lsgb_cli.cpp"), "-o", str(cli), "-ldl"],
+                       cli, [CSRC / "lsgb_cli.cpp"]))
     with cf.ThreadPoolExecutor(jobs) as ex:
         for f in [ex.submit(_run, c, force, o, d) for c, o, d in link_steps]:
             f.result()

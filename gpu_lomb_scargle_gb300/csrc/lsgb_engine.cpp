@@ -96,6 +96,7 @@ struct lsgb_engine {
     uint64_t last_units = 0;
     cudaEvent_t ev_main0 = nullptr, ev_main1 = nullptr;  // around the last main-kernel launch
     bool ev_valid = false;
+    uint32_t reanchor = 0;  // mixed form: 0 = anchor at each thread's frequency run
 };
 
 extern "C" {
@@ -162,6 +163,12 @@ LSGB_API int lsgb_set_tuning(lsgb_engine *eng, int variant, int f, int nt, int m
 }
 
 LSGB_API int lsgb_mixed_shapes(int *out, int max_shapes) { return mixed_shapes(out, max_shapes); }
+
+LSGB_API int lsgb_set_reanchor(lsgb_engine *eng, uint32_t interval) {
+    if (!eng) return fail(LSGB_ERR_INVALID, "lsgb_set_reanchor: engine is NULL");
+    eng->reanchor = interval;
+    return LSGB_OK;
+}
 
 LSGB_API int lsgb_get_tuning(lsgb_engine *eng, int variant, int *out5) {
     if (!eng || !out5 || (variant != 0 && variant != 1))
@@ -288,6 +295,7 @@ LSGB_API int lsgb_periodogram_device(lsgb_engine *eng, int variant, int precisio
         a.counter = (uint32_t *)eng->counter.p;
         a.pgram = pgram;
         a.tile_best = want_best ? (TileBest *)eng->tile_best.p : nullptr;
+        a.reanchor = eng->reanchor;
         const int grid = (int)std::min<uint64_t>((uint64_t)eng->sms * occ, n_units64);
         LSGB_CUDA(cudaEventRecord(eng->ev_main0, st));
         LSGB_CUDA(launch_mixed(variant, dtype, shape, a, grid, smem, st));

@@ -58,6 +58,8 @@ struct MixedArgs {
     uint32_t *counter;     // persistent work-queue head (zeroed before launch)
     void *pgram;           // [n_obj x n_freq] or null
     TileBest *tile_best;   // [n_obj x n_tiles] or null
+    uint32_t reanchor;     // 0: anchor at every thread's run start; R > 0: anchor every R
+                           // grid points and reach the run start by the FP32 recurrence
 };
 
 struct PlainArgs {

@@ -369,11 +369,24 @@ __global__ void __launch_bounds__(NT, MINB) mixed_kernel(MixedArgs a) {
 #pragma unroll 1
             for (uint32_t j = 0; j < cnt; ++j) {
                 const uint4 ab = X2 ? s_rec[4 * j] : s_rec[2 * j];
-                // anchor: top 32 bits of a + k0*b (mod 2^64), as a signed turn count
-                const uint64_t p = (uint64_t)k0 * ab.z + (((uint64_t)ab.y << 32) | ab.x);
-                const uint32_t hi = (uint32_t)(p >> 32) + k0 * ab.w;
+                // anchor: top 32 bits of a + ka*b (mod 2^64), as a signed turn count; ka is
+                // the thread's first frequency, or with re-anchoring every R grid points
+                // the R-aligned point below it
+                const uint32_t adv = a.reanchor ? k0 % a.reanchor : 0u;
+                const uint32_t ka = k0 - adv;
+                const uint64_t p = (uint64_t)ka * ab.z + (((uint64_t)ab.y << 32) | ab.x);
+                const uint32_t hi = (uint32_t)(p >> 32) + ka * ab.w;
                 float s, c;
                 __sincosf((float)(int32_t)hi * kTwoPiOver2p32f, &s, &c);
+                if (adv) {
+                    const float4 v = reinterpret_cast<const float4 *>(s_rec)[X2 ? 4 * j + 1 : 2 * j + 1];
+                    const float cd = v.z, sd = v.w;  // same place in both layouts
+                    for (uint32_t q = 0; q < adv; ++q) {
+                        const float cn = fmaf(c, cd, -s * sd);
+                        s = fmaf(s, cd, c * sd);
+                        c = cn;
+                    }
+                }
                 if (!X2) {
                     const float4 v = reinterpret_cast<const float4 *>(s_rec)[2 * j + 1];
 #pragma unroll

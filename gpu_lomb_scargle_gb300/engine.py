@@ -86,6 +86,9 @@ class Engine:
         self._check(self._lib.lsgb_set_tuning(self._h, variant, freqs_per_thread, threads,
                                               min_ctas, packed))
 
+    def set_reanchor(self, interval: int):
+        self._check(self._lib.lsgb_set_reanchor(self._h, int(interval)))
+
     def get_tuning(self, variant: int):
         out = (ctypes.c_int * 5)()
         self._check(self._lib.lsgb_get_tuning(self._h, variant, out))

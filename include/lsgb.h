@@ -123,9 +123,46 @@ LSGB_API int lsgb_periodogram_noalloc(int variant, int dtype, const void *t, con
                                       int normalize, void *pgram, uint32_t *best_idx,
                                       void *best_power, void *stream);
 
+/* ---- continuous-batching request loop (no counterpart in the reference, whose
+ * entry point is one synchronous batch per call, source/main.cu:742-941) ----
+ * Objects are submitted one at a time. A dispatcher thread packs whatever has
+ * arrived into the next free slot (up to max_batch_objects), admits the batch only
+ * while the device bytes of all in-flight batches stay under hbm_budget_bytes (a
+ * single object larger than the budget runs alone), and launches it on the slot's
+ * own stream and engine, so up to `slots` batches overlap on the GPU. Every object
+ * gets the best frequency index and power of its periodogram over one shared grid. */
+typedef struct lsgb_server lsgb_server;
+
+LSGB_API int lsgb_server_create(int device, int variant, int precision, double fmin, double df,
+                                uint32_t n_freq, int normalize, uint32_t slots,
+                                uint32_t max_batch_objects, uint64_t hbm_budget_bytes,
+                                lsgb_server **out);
+/* Copies the object's n observations (host doubles) into the queue; dy is read
+ * only for LSGB_GENERALIZED. Thread-safe. */
+LSGB_API int lsgb_server_submit(lsgb_server *srv, uint64_t id, const double *t, const double *y,
+                                const double *dy, uint32_t n);
+/* Up to max completed objects: id, best index, best power, submit and completion
+ * times (seconds, lsgb_server_now() clock). Returns the count, or a negative status
+ * once the loop has failed. */
+LSGB_API int lsgb_server_poll(lsgb_server *srv, uint32_t max, uint64_t *ids, uint32_t *best_idx,
+                              double *best_power, double *t_submit, double *t_done);
+/* [batches launched, objects completed, largest batch, objects waiting, peak
+ * in-flight device bytes] */
+LSGB_API int lsgb_server_stats(lsgb_server *srv, uint64_t *out5);
+LSGB_API double lsgb_server_now(void);
+/* Finishes every submitted object, then stops the loop and frees it. */
+LSGB_API void lsgb_server_destroy(lsgb_server *srv);
+
 /* The compiled mixed-kernel shapes, as out[5*i .. 5*i+4] = (variant, F, threads,
  * min CTAs per SM, packed), at most max_shapes of them. Returns how many exist. */
 LSGB_API int lsgb_mixed_shapes(int *out, int max_shapes);
+
+/* Re-anchoring interval R of the mixed form's recurrence. 0 (default): every thread's
+ * run of F frequencies starts from an exact anchor, so no frequency is more than F-1
+ * recurrence steps from one. R > 0: anchors only at multiples of R, each thread reaching
+ * its run by up to R-1 extra FP32 steps -- the error of an R-step recurrence, at extra
+ * cost; used to measure precision against R. */
+LSGB_API int lsgb_set_reanchor(lsgb_engine *eng, uint32_t interval);
 
 /* The shape the engine uses for a variant, in the same 5-int layout. */
 LSGB_API int lsgb_get_tuning(lsgb_engine *eng, int variant, int *out5);

@@ -1,0 +1,54 @@
+"""The continuous-batching request loop: every object's result is the same alone and in
+the mix, and agrees with the oracle."""
+import numpy as np
+import pytest
+
+from gpu_lomb_scargle_gb300 import engine as E
+from gpu_lomb_scargle_gb300 import serve, synth
+from oracle import pyoracle
+from tests.gpu_helpers import MIXED_ATOL
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("variant", [0, 1])
+def test_results_alone_equal_results_in_the_mix(native_libs, cuda_ok, variant):
+    st = synth.stream(seed=77 + variant, n_obj=500, rate_hz=5000.0, n_freq=20_000)
+    rng = np.random.default_rng(5)
+    objects = []
+    for i in range(500):
+        t, y = synth.stream_object(st, i)
+        dy = rng.uniform(0.01, 0.1, t.size) if variant else np.ones_like(t)
+        objects.append((t, y, dy))
+    report, res = serve.replay(st, variant=variant, slots=3, max_batch=64, objects=objects)
+    assert report["completed"] == 500
+    assert report["batches"] > 3  # arrivals were spread over several overlapping batches
+    eng = E.Engine(0)
+    df = (st.fmax - st.fmin) / st.n_freq
+    for i, (t, y, dy) in enumerate(objects):
+        alone = eng.run_host(variant, "mixed", t, y, dy if variant else None,
+                             np.array([0, t.size], np.uint64), st.fmin, df, st.n_freq,
+                             normalize=True)
+        assert res["ids"][i] == i
+        assert res["best_idx"][i] == alone.best_idx[0], i
+        assert res["best_power"][i] == alone.best_power[0], i
+    # and a sample against the oracle (grid indices around each best and a coarse sweep)
+    for i in range(0, 500, 50):
+        t, y, dy = objects[i]
+        if variant:
+            _, y = pyoracle.batch_pgram(1, t, y, dy, [0, t.size], st.fmin, df, n_freq=1)
+        kk = np.unique(np.concatenate([np.arange(0, st.n_freq, 97),
+                                       np.clip(res["best_idx"][i] + np.arange(-5, 6), 0,
+                                               st.n_freq - 1)]))
+        ref, _ = pyoracle.batch_pgram(variant, t, y, dy, [0, t.size], st.fmin, df, kidx=kk)
+        k = int(res["best_idx"][i])
+        assert abs(ref[0][np.searchsorted(kk, k)] - res["best_power"][i]) < MIXED_ATOL
+        assert ref[0].max() - ref[0][np.searchsorted(kk, k)] <= MIXED_ATOL
+
+
+def test_server_without_gpu_fails_loudly(native_libs):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(E.LsgbError) as ei:
+        serve.Server(1000, 1.0, 1e-3)
+    assert ei.value.status == -4
