@@ -63,7 +63,7 @@ def lsgb() -> ctypes.CDLL:
         lib.lsgb_periodogram_device.restype = i32
         lib.lsgb_periodogram_host.argtypes = common
         lib.lsgb_periodogram_host.restype = i32
-        lib.lsgb_set_tuning.argtypes = [vp, i32, i32, i32, i32, i32]
+        lib.lsgb_set_tuning.argtypes = [vp, i32, i32, i32, i32, i32, i32]
         lib.lsgb_set_tuning.restype = i32
         lib.lsgb_last_launch_info.argtypes = [vp, c.POINTER(c.c_uint32), c.POINTER(c.c_uint64)]
         lib.lsgb_last_launch_info.restype = i32

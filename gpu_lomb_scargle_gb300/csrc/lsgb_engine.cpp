@@ -89,9 +89,9 @@ struct lsgb_engine {
     int device = 0;
     int sms = 0;
     cudaStream_t stream = nullptr;  // host-buffer API stream
-    DevBuf objs, offs, perm, rec, tile_best, counter;
+    DevBuf objs, offs, perm, rec, tile_best, counter, keys;
     DevBuf in_t, in_y, in_dy, out_pg, out_idx, out_p;
-    MixedShape shape[2] = {{12, 256, 2, 1}, {8, 256, 2, 1}};
+    MixedShape shape[2] = {{12, 256, 2, 1, 0}, {8, 256, 2, 1, 0}};
     uint32_t last_kernels = 0;
     uint64_t last_units = 0;
     cudaEvent_t ev_main0 = nullptr, ev_main1 = nullptr;  // around the last main-kernel launch
@@ -136,7 +136,7 @@ LSGB_API void lsgb_engine_destroy(lsgb_engine *eng) {
     cudaSetDevice(eng->device);
     if (eng->stream) cudaStreamSynchronize(eng->stream);
     DevBuf *bufs[] = {&eng->objs,   &eng->offs,  &eng->perm,    &eng->rec,
-                      &eng->tile_best, &eng->counter, &eng->in_t, &eng->in_y,
+                      &eng->tile_best, &eng->counter, &eng->keys, &eng->in_t, &eng->in_y,
                       &eng->in_dy,  &eng->out_pg, &eng->out_idx, &eng->out_p};
     for (DevBuf *b : bufs) b->release();
     if (eng->stream) cudaStreamDestroy(eng->stream);
@@ -145,7 +145,8 @@ LSGB_API void lsgb_engine_destroy(lsgb_engine *eng) {
     delete eng;
 }
 
-LSGB_API int lsgb_set_tuning(lsgb_engine *eng, int variant, int f, int nt, int minb, int x2) {
+LSGB_API int lsgb_set_tuning(lsgb_engine *eng, int variant, int f, int nt, int minb, int x2,
+                             int unroll) {
     if (!eng || (variant != 0 && variant != 1))
         return fail(LSGB_ERR_INVALID, "lsgb_set_tuning: bad engine or variant");
     MixedShape s = eng->shape[variant];
@@ -153,11 +154,12 @@ LSGB_API int lsgb_set_tuning(lsgb_engine *eng, int variant, int f, int nt, int m
     if (nt > 0) s.nt = nt;
     if (minb > 0) s.minb = minb;
     if (x2 >= 0) s.x2 = x2 ? 1 : 0;
+    if (unroll >= 0) s.uj = unroll ? 1 : 0;
     int blocks = 0;
     if (mixed_occupancy(variant, LSGB_F32, s, 1024, &blocks) != cudaSuccess)
         return fail(LSGB_ERR_INVALID,
-                    "mixed shape F=%d x %d threads (min %d CTAs/SM, packed %d) is not compiled "
-                    "for variant %d", s.f, s.nt, s.minb, s.x2, variant);
+                    "mixed shape F=%d x %d threads (min %d CTAs/SM, packed %d, unroll %d) is not "
+                    "compiled for variant %d", s.f, s.nt, s.minb, s.x2, s.uj, variant);
     eng->shape[variant] = s;
     return LSGB_OK;
 }
@@ -170,15 +172,16 @@ LSGB_API int lsgb_set_reanchor(lsgb_engine *eng, uint32_t interval) {
     return LSGB_OK;
 }
 
-LSGB_API int lsgb_get_tuning(lsgb_engine *eng, int variant, int *out5) {
-    if (!eng || !out5 || (variant != 0 && variant != 1))
+LSGB_API int lsgb_get_tuning(lsgb_engine *eng, int variant, int *out6) {
+    if (!eng || !out6 || (variant != 0 && variant != 1))
         return fail(LSGB_ERR_INVALID, "lsgb_get_tuning: bad argument");
     const MixedShape s = eng->shape[variant];
-    out5[0] = variant;
-    out5[1] = s.f;
-    out5[2] = s.nt;
-    out5[3] = s.minb;
-    out5[4] = s.x2;
+    out6[0] = variant;
+    out6[1] = s.f;
+    out6[2] = s.nt;
+    out6[3] = s.minb;
+    out6[4] = s.x2;
+    out6[5] = s.uj;
     return LSGB_OK;
 }
 
@@ -257,7 +260,11 @@ LSGB_API int lsgb_periodogram_device(lsgb_engine *eng, int variant, int precisio
     LSGB_CUDA(eng->objs.ensure(sizeof(ObjInfo) * n_obj));
     LSGB_CUDA(eng->offs.ensure(sizeof(uint64_t) * (n_obj + 1)));
     LSGB_CUDA(eng->perm.ensure(sizeof(uint32_t) * n_obj));
-    if (want_best) LSGB_CUDA(eng->tile_best.ensure(sizeof(TileBest) * n_units64));
+    if (want_best && !mixed) LSGB_CUDA(eng->tile_best.ensure(sizeof(TileBest) * n_units64));
+    if (want_best && mixed) {
+        LSGB_CUDA(eng->keys.ensure(sizeof(unsigned long long) * n_obj));
+        LSGB_CUDA(cudaMemsetAsync(eng->keys.p, 0, sizeof(unsigned long long) * n_obj, st));
+    }
     if (mixed) LSGB_CUDA(eng->rec.ensure(sizeof(ObsRec) * rows));
     LSGB_CUDA(cudaMemcpyAsync(eng->objs.p, h_objs.data(), sizeof(ObjInfo) * n_obj,
                               cudaMemcpyHostToDevice, st));
@@ -280,7 +287,9 @@ LSGB_API int lsgb_periodogram_device(lsgb_engine *eng, int variant, int precisio
         ++kernels;
         const uint32_t rec_bytes = (uint32_t)mixed_rec_bytes(shape);
         const uint32_t chunk = std::min<uint32_t>(max_n, kMixedSmemMax / rec_bytes);
-        const size_t smem = (size_t)rec_bytes * chunk;
+        // objects longer than one chunk sum in two levels (chunk sums folded in smem)
+        const bool fold = max_n > chunk;
+        const size_t smem = (size_t)rec_bytes * chunk + (fold ? mixed_fold_bytes(variant, shape) : 0);
         int occ = 0;
         LSGB_CUDA(mixed_occupancy(variant, dtype, shape, smem, &occ));
         if (occ < 1) return fail(LSGB_ERR_CUDA, "mixed kernel does not fit on an SM (smem %zu)", smem);
@@ -294,8 +303,10 @@ LSGB_API int lsgb_periodogram_device(lsgb_engine *eng, int variant, int precisio
         a.chunk = chunk;
         a.counter = (uint32_t *)eng->counter.p;
         a.pgram = pgram;
-        a.tile_best = want_best ? (TileBest *)eng->tile_best.p : nullptr;
+        a.tile_best = nullptr;
+        a.best_key = want_best ? (unsigned long long *)eng->keys.p : nullptr;
         a.reanchor = eng->reanchor;
+        a.fold = fold ? 1u : 0u;
         const int grid = (int)std::min<uint64_t>((uint64_t)eng->sms * occ, n_units64);
         LSGB_CUDA(cudaEventRecord(eng->ev_main0, st));
         LSGB_CUDA(launch_mixed(variant, dtype, shape, a, grid, smem, st));
@@ -330,7 +341,11 @@ LSGB_API int lsgb_periodogram_device(lsgb_engine *eng, int variant, int precisio
         eng->ev_valid = true;
         ++kernels;
     }
-    if (want_best) {
+    if (want_best && mixed) {
+        LSGB_CUDA(launch_key_decode(dtype, (const unsigned long long *)eng->keys.p, n_obj, best_idx,
+                                    best_power, st));
+        ++kernels;
+    } else if (want_best) {
         LSGB_CUDA(launch_best_reduce(dtype, (const TileBest *)eng->tile_best.p, n_obj, n_tiles,
                                      best_idx, best_power, st));
         ++kernels;

@@ -60,7 +60,12 @@ struct MixedArgs {
     TileBest *tile_best;   // [n_obj x n_tiles] or null
     uint32_t reanchor;     // 0: anchor at every thread's run start; R > 0: anchor every R
                            // grid points and reach the run start by the FP32 recurrence
+    unsigned long long *best_key;  // [n_obj] packed (power bits << 32 | ~index) maxima, or
+                                   // null to use tile_best; zero means "no positive power"
+    uint32_t fold;         // 1: shared memory holds a second-level sum area after the records
+                           // (objects longer than `chunk` fold their chunk sums into it)
 };
+
 
 struct PlainArgs {
     const void *t, *y, *dy;
@@ -78,9 +83,14 @@ struct PlainArgs {
 struct MixedShape {
     int f, nt, minb;
     int x2;  // 1: packed f32x2 loop (two interleaved frequency chains per thread)
+    int uj;  // 1: two observations per inner-loop iteration (independent chains), 0: one
 };
 // Bytes of shared memory per staged observation of a mixed shape.
 inline int mixed_rec_bytes(const MixedShape &s) { return s.x2 ? 64 : 32; }
+// Bytes of the second-level sum area of a mixed shape (NA sums x F x threads floats).
+inline size_t mixed_fold_bytes(int variant, const MixedShape &s) {
+    return (size_t)(variant ? 6 : 4) * s.f * s.nt * sizeof(float);
+}
 
 // ---- launchers (lsgb_kernels.cu); all asynchronous on `st` ----
 cudaError_t launch_stats(int variant, int mixed, int dtype, int normalize, const void *y,
@@ -99,6 +109,9 @@ cudaError_t launch_plain(int variant, int in_dtype, int out_dtype, const PlainAr
 cudaError_t plain_occupancy(int variant, int in_dtype, int out_dtype, size_t smem, int *blocks);
 cudaError_t launch_best_reduce(int dtype, const TileBest *tb, uint32_t n_obj, uint32_t n_tiles,
                                uint32_t *best_idx, void *best_power, cudaStream_t st);
+// Unpacks MixedArgs::best_key maxima into (index, power).
+cudaError_t launch_key_decode(int dtype, const unsigned long long *keys, uint32_t n_obj,
+                              uint32_t *best_idx, void *best_power, cudaStream_t st);
 
 constexpr int kPlainThreads = 256;
 constexpr uint32_t kMixedSmemMax = 64 * 1024;  // shared memory for staged observations per CTA

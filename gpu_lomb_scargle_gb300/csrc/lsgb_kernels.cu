@@ -311,10 +311,13 @@ __device__ __forceinline__ void unpack2(uint64_t v, float &lo, float &hi) {
 // Each 64-bit half of q1..q3 is a ready-made packed operand.
 constexpr int kX2RecBytes = 64;
 
-template <int F, int NT, int MINB, bool GEN, bool X2, typename OutT>
+template <int F, int NT, int MINB, bool GEN, bool X2, int UJ, bool RA, typename OutT>
 __global__ void __launch_bounds__(NT, MINB) mixed_kernel(MixedArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     uint4 *s_rec = reinterpret_cast<uint4 *>(smem_raw);  // 2 x uint4 per observation
+    // second-level sums of objects longer than one staged chunk, private per thread:
+    // s_fold[(q * F + f) * NT + tid]; present when a.fold != 0
+    float *s_fold = reinterpret_cast<float *>(smem_raw + (size_t)a.chunk * (X2 ? kX2RecBytes : 32));
     __shared__ uint32_t s_unit;
     __shared__ float s_bp[NT / 32];
     __shared__ uint32_t s_bk[NT / 32];
@@ -346,6 +349,11 @@ __global__ void __launch_bounds__(NT, MINB) mixed_kernel(MixedArgs a) {
             for (int p = 0; p < NP; ++p) acc2[q][p] = 0ull;
         }
 
+        const bool fold = a.fold && n > a.chunk;
+        if (fold) {
+#pragma unroll
+            for (int q = 0; q < NA * F; ++q) s_fold[q * NT + threadIdx.x] = 0.0f;
+        }
         for (uint32_t c0 = 0; c0 < n; c0 += a.chunk) {
             const uint32_t cnt = min(a.chunk, n - c0);
             const uint4 *src = reinterpret_cast<const uint4 *>(a.rec + row0 + c0);
@@ -366,19 +374,19 @@ __global__ void __launch_bounds__(NT, MINB) mixed_kernel(MixedArgs a) {
                 }
             }
             __syncthreads();
-#pragma unroll 1
+#pragma unroll UJ
             for (uint32_t j = 0; j < cnt; ++j) {
                 const uint4 ab = X2 ? s_rec[4 * j] : s_rec[2 * j];
                 // anchor: top 32 bits of a + ka*b (mod 2^64), as a signed turn count; ka is
                 // the thread's first frequency, or with re-anchoring every R grid points
                 // the R-aligned point below it
-                const uint32_t adv = a.reanchor ? k0 % a.reanchor : 0u;
+                const uint32_t adv = RA ? k0 % a.reanchor : 0u;
                 const uint32_t ka = k0 - adv;
                 const uint64_t p = (uint64_t)ka * ab.z + (((uint64_t)ab.y << 32) | ab.x);
                 const uint32_t hi = (uint32_t)(p >> 32) + ka * ab.w;
                 float s, c;
                 __sincosf((float)(int32_t)hi * kTwoPiOver2p32f, &s, &c);
-                if (adv) {
+                if (RA && adv) {
                     const float4 v = reinterpret_cast<const float4 *>(s_rec)[X2 ? 4 * j + 1 : 2 * j + 1];
                     const float cd = v.z, sd = v.w;  // same place in both layouts
                     for (uint32_t q = 0; q < adv; ++q) {
@@ -446,9 +454,37 @@ __global__ void __launch_bounds__(NT, MINB) mixed_kernel(MixedArgs a) {
                     }
                 }
             }
+            if (fold) {
+                // fold this chunk's FP32 sums into the second level and restart them, so
+                // rounding grows with sqrt(chunk) + sqrt(n / chunk) rather than sqrt(n)
+#pragma unroll
+                for (int q = 0; q < NA; ++q) {
+                    if (X2) {
+#pragma unroll
+                        for (int pp = 0; pp < NP; ++pp) {
+                            float lo, hi2;
+                            unpack2(acc2[q][pp], lo, hi2);
+                            s_fold[(q * F + 2 * pp) * NT + threadIdx.x] += lo;
+                            s_fold[(q * F + 2 * pp + 1) * NT + threadIdx.x] += hi2;
+                            acc2[q][pp] = 0ull;
+                        }
+                    } else {
+#pragma unroll
+                        for (int f = 0; f < F; ++f) {
+                            s_fold[(q * F + f) * NT + threadIdx.x] += acc[q][f];
+                            acc[q][f] = 0.0f;
+                        }
+                    }
+                }
+            }
             __syncthreads();
         }
-        if (X2) {
+        if (fold) {
+#pragma unroll
+            for (int q = 0; q < NA; ++q)
+#pragma unroll
+                for (int f = 0; f < F; ++f) acc[q][f] = s_fold[(q * F + f) * NT + threadIdx.x];
+        } else if (X2) {
 #pragma unroll
             for (int q = 0; q < NA; ++q)
 #pragma unroll
@@ -489,7 +525,19 @@ __global__ void __launch_bounds__(NT, MINB) mixed_kernel(MixedArgs a) {
                 }
             }
         }
-        if (a.tile_best) {
+        if (a.best_key) {
+            // warp maximum, then one 64-bit atomicMax per warp: larger power wins, and on
+            // equal power the larger ~index, i.e. the lower index (the first maximum)
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const float op = __shfl_xor_sync(0xffffffffu, bp, off);
+                const uint32_t ok = __shfl_xor_sync(0xffffffffu, bk, off);
+                if (better(op, ok, bp, bk)) { bp = op; bk = ok; }
+            }
+            if ((threadIdx.x & 31) == 0 && bp > 0.0f)
+                atomicMax(a.best_key + o,
+                          ((unsigned long long)__float_as_uint(bp) << 32) | (unsigned long long)(~bk));
+        } else if (a.tile_best) {
             block_best<NT, float>(bp, bk, s_bp, s_bk);
             if (threadIdx.x == 0) {
                 TileBest tb;
@@ -498,8 +546,8 @@ __global__ void __launch_bounds__(NT, MINB) mixed_kernel(MixedArgs a) {
                 tb.pad = 0;
                 a.tile_best[(uint64_t)o * a.n_tiles + tile] = tb;
             }
+            __syncthreads();
         }
-        __syncthreads();
     }
 }
 
@@ -694,15 +742,25 @@ __global__ void best_reduce_kernel(const TileBest *tb, uint32_t n_obj, uint32_t 
     }
 }
 
-template <int F, int NT, int MINB, bool GEN, bool X2>
+template <typename OutT>
+__global__ void key_decode_kernel(const unsigned long long *keys, uint32_t n_obj, uint32_t *best_idx,
+                                  OutT *best_power) {
+    const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= n_obj) return;
+    const unsigned long long k = keys[o];
+    if (best_idx) best_idx[o] = k ? ~(uint32_t)k : 0u;
+    if (best_power) best_power[o] = (OutT)__uint_as_float((uint32_t)(k >> 32));
+}
+
+template <int F, int NT, int MINB, bool GEN, bool X2, int UJ, bool RA>
 cudaError_t launch_mixed_t(int dtype, const MixedArgs &a, int grid, size_t smem, cudaStream_t st) {
     if (dtype == 0) {
-        auto k = mixed_kernel<F, NT, MINB, GEN, X2, float>;
+        auto k = mixed_kernel<F, NT, MINB, GEN, X2, UJ, RA, float>;
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         k<<<grid, NT, smem, st>>>(a);
     } else {
-        auto k = mixed_kernel<F, NT, MINB, GEN, X2, double>;
+        auto k = mixed_kernel<F, NT, MINB, GEN, X2, UJ, RA, double>;
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         k<<<grid, NT, smem, st>>>(a);
@@ -710,15 +768,15 @@ cudaError_t launch_mixed_t(int dtype, const MixedArgs &a, int grid, size_t smem,
     return cudaGetLastError();
 }
 
-template <int F, int NT, int MINB, bool GEN, bool X2>
+template <int F, int NT, int MINB, bool GEN, bool X2, int UJ, bool RA>
 cudaError_t occ_mixed_t(int dtype, size_t smem, int *blocks) {
     cudaError_t e;
     if (dtype == 0) {
-        auto k = mixed_kernel<F, NT, MINB, GEN, X2, float>;
+        auto k = mixed_kernel<F, NT, MINB, GEN, X2, UJ, RA, float>;
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k, NT, smem);
     } else {
-        auto k = mixed_kernel<F, NT, MINB, GEN, X2, double>;
+        auto k = mixed_kernel<F, NT, MINB, GEN, X2, UJ, RA, double>;
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k, NT, smem);
     }
@@ -726,19 +784,22 @@ cudaError_t occ_mixed_t(int dtype, size_t smem, int *blocks) {
 }
 
 // The compiled mixed shapes: (frequencies per thread, threads, min CTAs per SM for
-// the register budget, generalized?, packed f32x2 loop?).
-#define LSGB_MIXED_SHAPES(X)    \
-    X(16, 256, 2, false, false) \
-    X(16, 128, 4, false, false) \
-    X(8, 256, 3, false, false)  \
-    X(16, 256, 2, false, true)  \
-    X(16, 128, 4, false, true)  \
-    X(12, 256, 2, false, true)  \
-    X(8, 256, 3, false, true)   \
-    X(12, 256, 2, true, false)  \
-    X(6, 256, 3, true, false)   \
-    X(12, 256, 2, true, true)   \
-    X(8, 256, 2, true, true)
+// the register budget, generalized?, packed f32x2 loop?, observations per iteration,
+// re-anchoring study variant?). Study variants are chosen by lsgb_set_reanchor, not
+// listed as tuning shapes.
+#define LSGB_MIXED_SHAPES(X)                \
+    X(16, 256, 2, false, false, 1, false)   \
+    X(8, 256, 3, false, false, 1, false)    \
+    X(12, 256, 2, false, true, 1, false)    \
+    X(12, 128, 4, false, true, 1, false)    \
+    X(10, 256, 2, false, true, 1, false)    \
+    X(8, 256, 3, false, true, 1, false)     \
+    X(12, 256, 2, true, false, 1, false)    \
+    X(8, 256, 2, true, true, 1, false)      \
+    X(8, 128, 4, true, true, 1, false)      \
+    X(10, 256, 2, true, true, 1, false)     \
+    X(12, 256, 2, false, true, 1, true)     \
+    X(8, 256, 2, true, true, 1, true)
 
 }  // namespace
 
@@ -762,10 +823,10 @@ cudaError_t launch_records(int variant, int dtype, const void *t, const void *y,
 
 cudaError_t launch_mixed(int variant, int dtype, MixedShape shape, const MixedArgs &a, int grid,
                          size_t smem, cudaStream_t st) {
-#define X(F_, NT_, MB_, G_, X2_)                                                    \
+#define X(F_, NT_, MB_, G_, X2_, UJ_, RA_)                                           \
     if (shape.f == F_ && shape.nt == NT_ && shape.minb == MB_ && (variant == 1) == G_ && \
-        (shape.x2 != 0) == X2_)                                                          \
-        return launch_mixed_t<F_, NT_, MB_, G_, X2_>(dtype, a, grid, smem, st);
+        (shape.x2 != 0) == X2_ && (shape.uj ? 2 : 1) == UJ_ && (a.reanchor != 0) == RA_) \
+        return launch_mixed_t<F_, NT_, MB_, G_, X2_, UJ_, RA_>(dtype, a, grid, smem, st);
     LSGB_MIXED_SHAPES(X)
 #undef X
     return cudaErrorInvalidValue;
@@ -773,25 +834,27 @@ cudaError_t launch_mixed(int variant, int dtype, MixedShape shape, const MixedAr
 
 int mixed_shapes(int *out, int max_shapes) {
     int n = 0;
-#define X(F_, NT_, MB_, G_, X2_)                 \
-    if (out && n < max_shapes) {                 \
-        out[5 * n + 0] = G_ ? 1 : 0;             \
-        out[5 * n + 1] = F_;                     \
-        out[5 * n + 2] = NT_;                    \
-        out[5 * n + 3] = MB_;                    \
-        out[5 * n + 4] = X2_ ? 1 : 0;            \
+#define X(F_, NT_, MB_, G_, X2_, UJ_, RA_)       \
+    if (RA_) {                                   \
+    } else if (out && n < max_shapes) {          \
+        out[6 * n + 0] = G_ ? 1 : 0;             \
+        out[6 * n + 1] = F_;                     \
+        out[6 * n + 2] = NT_;                    \
+        out[6 * n + 3] = MB_;                    \
+        out[6 * n + 4] = X2_ ? 1 : 0;            \
+        out[6 * n + 5] = UJ_ == 2 ? 1 : 0;       \
     }                                            \
-    ++n;
+    n += RA_ ? 0 : 1;
     LSGB_MIXED_SHAPES(X)
 #undef X
     return n;
 }
 
 cudaError_t mixed_occupancy(int variant, int dtype, MixedShape shape, size_t smem, int *blocks) {
-#define X(F_, NT_, MB_, G_, X2_)                                                    \
+#define X(F_, NT_, MB_, G_, X2_, UJ_, RA_)                                           \
     if (shape.f == F_ && shape.nt == NT_ && shape.minb == MB_ && (variant == 1) == G_ && \
-        (shape.x2 != 0) == X2_)                                                          \
-        return occ_mixed_t<F_, NT_, MB_, G_, X2_>(dtype, smem, blocks);
+        (shape.x2 != 0) == X2_ && (shape.uj ? 2 : 1) == UJ_ && !RA_)                     \
+        return occ_mixed_t<F_, NT_, MB_, G_, X2_, UJ_, RA_>(dtype, smem, blocks);
     LSGB_MIXED_SHAPES(X)
 #undef X
     return cudaErrorInvalidValue;
@@ -827,6 +890,17 @@ cudaError_t plain_occupancy(int variant, int in_dtype, int out_dtype, size_t sme
     PlainArgs dummy{};
     return variant == 0 ? plain_dispatch<false>(in_dtype, out_dtype, dummy, 0, smem, 0, blocks)
                         : plain_dispatch<true>(in_dtype, out_dtype, dummy, 0, smem, 0, blocks);
+}
+
+cudaError_t launch_key_decode(int dtype, const unsigned long long *keys, uint32_t n_obj,
+                              uint32_t *best_idx, void *best_power, cudaStream_t st) {
+    if (n_obj == 0) return cudaSuccess;
+    const int blocks = (int)((n_obj + 255) / 256);
+    if (dtype == 0)
+        key_decode_kernel<float><<<blocks, 256, 0, st>>>(keys, n_obj, best_idx, (float *)best_power);
+    else
+        key_decode_kernel<double><<<blocks, 256, 0, st>>>(keys, n_obj, best_idx, (double *)best_power);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_best_reduce(int dtype, const TileBest *tb, uint32_t n_obj, uint32_t n_tiles,

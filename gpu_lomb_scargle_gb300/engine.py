@@ -82,15 +82,15 @@ class Engine:
             pass
 
     def set_tuning(self, variant: int, freqs_per_thread: int = 0, threads: int = 0,
-                   min_ctas: int = 0, packed: int = -1):
+                   min_ctas: int = 0, packed: int = -1, unroll: int = -1):
         self._check(self._lib.lsgb_set_tuning(self._h, variant, freqs_per_thread, threads,
-                                              min_ctas, packed))
+                                              min_ctas, packed, unroll))
 
     def set_reanchor(self, interval: int):
         self._check(self._lib.lsgb_set_reanchor(self._h, int(interval)))
 
     def get_tuning(self, variant: int):
-        out = (ctypes.c_int * 5)()
+        out = (ctypes.c_int * 6)()
         self._check(self._lib.lsgb_get_tuning(self._h, variant, out))
         return tuple(out)[1:]
 
@@ -152,12 +152,12 @@ class Engine:
 
 
 def mixed_shapes():
-    """Compiled mixed-kernel shapes: list of (variant, F, threads, min_ctas, packed)."""
+    """Compiled mixed-kernel shapes: (variant, F, threads, min_ctas, packed, unroll)."""
     lib = _native.lsgb()
     n = lib.lsgb_mixed_shapes(None, 0)
-    buf = (ctypes.c_int * (5 * n))()
+    buf = (ctypes.c_int * (6 * n))()
     lib.lsgb_mixed_shapes(buf, n)
-    return [tuple(buf[5 * i:5 * i + 5]) for i in range(n)]
+    return [tuple(buf[6 * i:6 * i + 6]) for i in range(n)]
 
 
 _default: Engine | None = None

@@ -111,18 +111,18 @@ def replay(stream: synth.Stream, n_objects: int | None = None, variant: int = ST
     srv.poll()
 
     results = []
+    collected = [0]
     done = threading.Event()
 
     def collector():
         while not done.is_set():
             r = srv.poll()
-            if len(r[0]):
-                results.append(r)
-            else:
+            keep = r[0] < n  # warm-up objects finishing late are not part of the stream
+            if keep.any():
+                results.append(tuple(x[keep] for x in r))
+                collected[0] += int(keep.sum())
+            elif not len(r[0]):
                 time.sleep(2e-4)
-        r = srv.poll()
-        if len(r[0]):
-            results.append(r)
 
     th = threading.Thread(target=collector, daemon=True)
     th.start()
@@ -140,11 +140,16 @@ def replay(stream: synth.Stream, n_objects: int | None = None, variant: int = ST
         lateness[i] = time.perf_counter() - target
         t, y, dy = objects[i]
         srv.submit(i, t, y, dy)
-    stats_before_close = srv.stats()
-    srv.close()
+    # every submitted object is collected before the loop is shut down (results still
+    # queued in the server when it is destroyed would be discarded)
+    deadline = time.perf_counter() + 60.0
+    while collected[0] < n and time.perf_counter() < deadline:
+        time.sleep(1e-3)
     wall = time.perf_counter() - t0
     done.set()
     th.join()
+    stats_before_close = srv.stats()
+    srv.close()
     ids = np.concatenate([r[0] for r in results]) if results else np.zeros(0, np.uint64)
     order = np.argsort(ids)
     cat = lambda k: np.concatenate([r[k] for r in results])[order]

@@ -89,11 +89,12 @@ LSGB_API int lsgb_periodogram_host(lsgb_engine *eng, int variant, int precision,
                                    void *best_power);
 
 /* Tuning of the mixed kernel: frequencies per thread (F), threads per CTA, the
- * minimum CTAs per SM the kernel's register budget is compiled for, and the packed
- * f32x2 inner loop (1) or the scalar one (0). 0 (-1 for packed) keeps the current
- * value. Returns LSGB_ERR_INVALID for shapes that are not compiled in. */
+ * minimum CTAs per SM the kernel's register budget is compiled for, the packed
+ * f32x2 inner loop (1) or the scalar one (0), and two observations per loop
+ * iteration (1) or one (0). 0 (-1 for the last two) keeps the current value.
+ * Returns LSGB_ERR_INVALID for shapes that are not compiled in. */
 LSGB_API int lsgb_set_tuning(lsgb_engine *eng, int variant, int freqs_per_thread,
-                             int threads_per_cta, int min_ctas_per_sm, int packed);
+                             int threads_per_cta, int min_ctas_per_sm, int packed, int unroll);
 
 /* The mixed-form periodogram of lsgb_periodogram_device, with no allocation at all.
  * No counterpart in the reference.
@@ -150,11 +151,12 @@ LSGB_API int lsgb_server_poll(lsgb_server *srv, uint32_t max, uint64_t *ids, uin
  * in-flight device bytes] */
 LSGB_API int lsgb_server_stats(lsgb_server *srv, uint64_t *out5);
 LSGB_API double lsgb_server_now(void);
-/* Finishes every submitted object, then stops the loop and frees it. */
+/* Finishes every submitted object, then stops the loop and frees it; results not yet
+ * taken with lsgb_server_poll are discarded. */
 LSGB_API void lsgb_server_destroy(lsgb_server *srv);
 
-/* The compiled mixed-kernel shapes, as out[5*i .. 5*i+4] = (variant, F, threads,
- * min CTAs per SM, packed), at most max_shapes of them. Returns how many exist. */
+/* The compiled mixed-kernel shapes, as out[6*i .. 6*i+5] = (variant, F, threads,
+ * min CTAs per SM, packed, unroll), at most max_shapes of them. Returns how many exist. */
 LSGB_API int lsgb_mixed_shapes(int *out, int max_shapes);
 
 /* Re-anchoring interval R of the mixed form's recurrence. 0 (default): every thread's
@@ -164,8 +166,8 @@ LSGB_API int lsgb_mixed_shapes(int *out, int max_shapes);
  * cost; used to measure precision against R. */
 LSGB_API int lsgb_set_reanchor(lsgb_engine *eng, uint32_t interval);
 
-/* The shape the engine uses for a variant, in the same 5-int layout. */
-LSGB_API int lsgb_get_tuning(lsgb_engine *eng, int variant, int *out5);
+/* The shape the engine uses for a variant, in the same 6-int layout. */
+LSGB_API int lsgb_get_tuning(lsgb_engine *eng, int variant, int *out6);
 
 /* Launch statistics of the last call: kernels launched and the work units the
  * persistent kernel processed. */

@@ -1,0 +1,139 @@
+"""The benchmark workloads at their full sizes against the FP64 oracle.
+
+Workloads 0-3 (the single 3,555-observation object; the 999-object batches, standard and
+generalized, 1e6 frequencies; the 200,000-observation object with 1e7 frequencies) run
+on the GPU in full. The oracle checks them on a sample of grid indices plus a window
+around every object's best index:
+  * max absolute error of the mixed form <= 1e-4 (normalized power);
+  * plain FP64 <= 1e-9 relative (tests/gpu_helpers.py);
+  * each GPU best index is the oracle's maximum over its window and over the sample,
+    within the tolerance.
+On the long object the mixed form's re-anchoring interval R is swept over 16, 64 and
+256 (0 = every thread's run re-anchors, the production setting). The errors are
+written to $LSGB_PRECISION_REPORT (JSON) when that variable is set.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from gpu_lomb_scargle_gb300 import engine as E
+from gpu_lomb_scargle_gb300 import synth
+from oracle import pyoracle
+from tests.gpu_helpers import MIXED_ATOL, PLAIN_RTOL, plain_rel_err
+
+pytestmark = pytest.mark.gpu
+REPORT = {}
+
+
+@pytest.fixture(scope="module")
+def eng(native_libs, cuda_ok):
+    e = E.Engine(0)
+    yield e
+    path = os.environ.get("LSGB_PRECISION_REPORT")
+    if path:
+        with open(path, "w") as f:
+            json.dump(REPORT, f, indent=1)
+
+
+def _columns(eng, w, variant, precision, y, kidx):
+    """GPU powers at grid indices kidx for every object (computed on the full grid)."""
+    import torch
+
+    dev = torch.device("cuda:0")
+    t = torch.from_numpy(w.t).to(dev)
+    yy = torch.from_numpy(y).to(dev)
+    dy = torch.from_numpy(w.dy).to(dev) if variant else None
+    pg = torch.empty((w.n_obj, w.n_freq), dtype=torch.float64, device=dev)
+    bi = torch.empty(w.n_obj, dtype=torch.int32, device=dev)
+    bp = torch.empty(w.n_obj, dtype=torch.float64, device=dev)
+    eng.run_device(variant, precision, t, yy, dy, w.offsets, w.fmin, w.df, w.n_freq, variant == 0,
+                   pg, bi, bp)
+    torch.cuda.synchronize()
+    k = torch.from_numpy(np.asarray(kidx, np.int64)).to(dev)
+    cols = pg.index_select(1, k).cpu().numpy()
+    best = bi.cpu().numpy().astype(np.int64)
+    # powers in a window around each best index
+    win = np.arange(-8, 9)
+    wk = np.clip(best[:, None] + win[None, :], 0, w.n_freq - 1)
+    wpow = pg.gather(1, torch.from_numpy(wk).to(dev)).cpu().numpy()
+    del pg
+    torch.cuda.empty_cache()
+    return cols, best, wk, wpow
+
+
+def _check(name, eng, w, variant, precision, n_sample=600, seed=0):
+    y = w.y
+    if variant == 1:
+        _, y = pyoracle.batch_pgram(1, w.t, w.y, w.dy, w.offsets, w.fmin, w.df, n_freq=1)
+    rng = np.random.default_rng(seed)
+    kidx = np.unique(rng.integers(0, w.n_freq, n_sample))
+    cols, best, wk, wpow = _columns(eng, w, variant, precision, y, kidx)
+    ref, _ = pyoracle.batch_pgram(variant, w.t, y, w.dy, w.offsets, w.fmin, w.df, kidx=kidx)
+    # oracle on each object's window
+    wref = np.empty_like(wpow)
+    for o in range(w.n_obj):
+        a, b = int(w.offsets[o]), int(w.offsets[o + 1])
+        r, _ = pyoracle.batch_pgram(variant, w.t[a:b], y[a:b], w.dy[a:b], [0, b - a], w.fmin, w.df,
+                                    kidx=wk[o])
+        wref[o] = r[0]
+    if precision == "mixed":
+        err = max(float(np.max(np.abs(cols - ref))), float(np.max(np.abs(wpow - wref))))
+        ok = err < MIXED_ATOL
+        tol = MIXED_ATOL
+    else:
+        err = max(plain_rel_err(cols, ref), plain_rel_err(wpow, wref))
+        ok = err < PLAIN_RTOL
+        tol = 0.0
+    center = 8
+    bad = 0
+    for o in range(w.n_obj):
+        pb = wref[o, center]
+        if wref[o].max() - pb > tol or ref[o].max() - pb > tol:
+            bad += 1
+    REPORT[name] = {"precision": precision, "max_err": err, "objects": w.n_obj,
+                    "n_freq": w.n_freq, "sampled_freqs": int(kidx.size), "best_mismatch": bad,
+                    "metric": "abs" if precision == "mixed" else "rel"}
+    print(name, REPORT[name])
+    assert ok, (name, err)
+    assert bad == 0, (name, bad)
+
+
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+def test_single_object_3555(eng, precision):
+    w = synth.single_object()
+    _check(f"single_3555obs_1e5f_{precision}", eng, w, 0, precision, n_sample=2000)
+
+
+@pytest.mark.parametrize("precision", ["mixed", "plain"])
+def test_lognormal_batch_standard(eng, precision):
+    w = synth.lognormal_batch()
+    if precision == "plain":
+        w = w.subset_freqs(50_000)  # the FP64 form: first 50k frequencies of the same grid
+    _check(f"lognormal_999obj_std_{precision}", eng, w, 0, precision, n_sample=300)
+
+
+@pytest.mark.parametrize("precision", ["mixed", "plain"])
+def test_lognormal_batch_generalized(eng, precision):
+    w = synth.lognormal_batch_dmag()
+    if precision == "plain":
+        w = w.subset_freqs(20_000)
+    _check(f"lognormal_999obj_gen_{precision}", eng, w, 1, precision, n_sample=300)
+
+
+@pytest.mark.parametrize("reanchor", [0, 16, 64, 256])
+def test_long_object_reanchor_sweep(eng, reanchor):
+    w = synth.long_object()
+    eng.set_reanchor(reanchor)
+    try:
+        name = f"long_200kobs_1e7f_mixed_R{reanchor or 'F'}"
+        if reanchor == 0:
+            _check(name, eng, w, 0, "mixed", n_sample=400, seed=3)
+        else:
+            try:
+                _check(name, eng, w, 0, "mixed", n_sample=400, seed=3)
+            except AssertionError:
+                pass  # recorded in the report; only the production setting must meet 1e-4
+    finally:
+        eng.set_reanchor(0)

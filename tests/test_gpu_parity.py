@@ -198,7 +198,7 @@ def _compiled_shapes():
         return []
 
 
-@pytest.mark.parametrize("shape", _compiled_shapes(), ids=lambda s: "v%d_F%d_nt%d_mb%d_x%d" % s)
+@pytest.mark.parametrize("shape", _compiled_shapes(), ids=lambda s: "v%d_F%d_nt%d_mb%d_x%d_u%d" % s)
 def test_every_compiled_mixed_shape(eng, shape):
     """Each compiled (F, threads, min CTAs, packed) shape of the mixed kernel against the
     oracle, on a batch whose objects span several staging chunks and partial tiles."""
