@@ -20,7 +20,7 @@ LSGB_SYMBOLS = ("lsgb_engine_create", "lsgb_engine_destroy", "lsgb_last_error", 
                 "lsgb_last_launch_info", "lsgb_last_kernel_time", "lsgb_mixed_shapes",
                 "lsgb_get_tuning", "lsgb_periodogram_noalloc", "lsgb_server_create",
                 "lsgb_server_submit", "lsgb_server_poll", "lsgb_server_stats", "lsgb_server_now",
-                "lsgb_server_destroy", "lsgb_set_reanchor")
+                "lsgb_server_destroy", "lsgb_set_reanchor", "lsgb_fp64_sincos_check")
 PYABI_SYMBOLS = ("LombScarglePy", "LombScarglePy_last_status")
 
 
@@ -91,5 +91,7 @@ def lsgb() -> ctypes.CDLL:
         lib.lsgb_server_destroy.restype = None
         lib.lsgb_set_reanchor.argtypes = [vp, u32]
         lib.lsgb_set_reanchor.restype = i32
+        lib.lsgb_fp64_sincos_check.argtypes = [vp, u32, dbl, c.POINTER(c.c_double)]
+        lib.lsgb_fp64_sincos_check.restype = i32
         lib._lsgb_typed = True
     return lib

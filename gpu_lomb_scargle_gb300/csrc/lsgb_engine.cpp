@@ -166,6 +166,19 @@ LSGB_API int lsgb_set_tuning(lsgb_engine *eng, int variant, int f, int nt, int m
 
 LSGB_API int lsgb_mixed_shapes(int *out, int max_shapes) { return mixed_shapes(out, max_shapes); }
 
+LSGB_API int lsgb_fp64_sincos_check(lsgb_engine *eng, uint32_t n, double scale, double *max_err) {
+    if (!eng || !max_err) return fail(LSGB_ERR_INVALID, "lsgb_fp64_sincos_check: NULL argument");
+    LSGB_CUDA(cudaSetDevice(eng->device));
+    DevBuf d;
+    LSGB_CUDA(d.ensure(sizeof(double)));
+    LSGB_CUDA(cudaMemsetAsync(d.p, 0, sizeof(double), eng->stream));
+    LSGB_CUDA(launch_sincos_check(n, 12345, scale, (double *)d.p, eng->stream));
+    LSGB_CUDA(cudaMemcpyAsync(max_err, d.p, sizeof(double), cudaMemcpyDeviceToHost, eng->stream));
+    LSGB_CUDA(cudaStreamSynchronize(eng->stream));
+    d.release();
+    return LSGB_OK;
+}
+
 LSGB_API int lsgb_set_reanchor(lsgb_engine *eng, uint32_t interval) {
     if (!eng) return fail(LSGB_ERR_INVALID, "lsgb_set_reanchor: engine is NULL");
     eng->reanchor = interval;

@@ -109,6 +109,10 @@ cudaError_t launch_plain(int variant, int in_dtype, int out_dtype, const PlainAr
 cudaError_t plain_occupancy(int variant, int in_dtype, int out_dtype, size_t smem, int *blocks);
 cudaError_t launch_best_reduce(int dtype, const TileBest *tb, uint32_t n_obj, uint32_t n_tiles,
                                uint32_t *best_idx, void *best_power, cudaStream_t st);
+// Largest |difference| of the plain kernel's FP64 sine/cosine from sincos() over n
+// arguments spread over [-scale, scale]; *max_err (device) must start at 0.
+cudaError_t launch_sincos_check(uint32_t n, uint64_t seed, double scale, double *max_err,
+                                cudaStream_t st);
 // Unpacks MixedArgs::best_key maxima into (index, power).
 cudaError_t launch_key_decode(int dtype, const unsigned long long *keys, uint32_t n_obj,
                               uint32_t *best_idx, void *best_power, cudaStream_t st);

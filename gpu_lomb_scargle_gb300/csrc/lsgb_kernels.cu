@@ -551,6 +551,79 @@ __global__ void __launch_bounds__(NT, MINB) mixed_kernel(MixedArgs a) {
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// FP64 sine and cosine for the plain kernel, written for the FP64 pipe of this part
+// (1/64 of the FP32 rate), from published methods:
+//  * Cody & Waite argument reduction (Software Manual for the Elementary Functions,
+//    1980) modulo pi/64, with pi/64 as a double-double (FMA makes n*C1 exact enough for
+//    |x| < 2^34 * pi/64) and the integer n obtained by the 1.5*2^52 rounding trick;
+//  * a table of sin/cos(j pi/64), j = 0..127 (Tang's table-driven scheme), built per CTA
+//    in shared memory with sincospi;
+//  * Taylor polynomials on |r| <= pi/128: sin to r^7 (next term < 9e-21) and cos to r^6
+//    (next term < 3.3e-18, under half an ulp of 1);
+//  * sin(a+r) = sin a cos r + cos a sin r, cos(a+r) = cos a cos r - sin a sin r.
+// About 16 FP64 operations against roughly twice that for the general-purpose
+// sincos(). Arguments with |x| > 1e9 rad use sincos(). Checked against sincos() by
+// lsgb_fp64_sincos_check.
+// ---------------------------------------------------------------------------
+constexpr double kPiOver64Hi = 0.04908738521234052;
+constexpr double kPiOver64Lo = 1.9135106236677394e-18;
+constexpr double k64OverPi = 20.371832715762604;
+constexpr double kRoundMagic = 6755399441055744.0;  // 1.5 * 2^52
+
+__device__ __forceinline__ void table_sincos(double x, const double2 *tab, double *s, double *c) {
+    if (fabs(x) > 1.0e9) {
+        sincos(x, s, c);
+        return;
+    }
+    const double nm = fma(x, k64OverPi, kRoundMagic);
+    const int j = __double2loint(nm) & 127;
+    const double n = nm - kRoundMagic;
+    const double r = fma(-n, kPiOver64Lo, fma(-n, kPiOver64Hi, x));
+    const double r2 = r * r;
+    const double sp = fma(r2, fma(r2, -0.0001984126984126984, 0.008333333333333333),
+                          -0.16666666666666666);
+    const double sr = fma(r * r2, sp, r);
+    const double cr = fma(r2, fma(r2, fma(r2, -0.001388888888888889, 0.041666666666666664), -0.5),
+                          1.0);
+    const double2 t = tab[j];  // (sin, cos) of j pi/64
+    *s = fma(t.x, cr, t.y * sr);
+    *c = fma(t.y, cr, -(t.x * sr));
+}
+
+__device__ __forceinline__ void fill_sincos_table(double2 *tab) {
+    for (int j = threadIdx.x; j < 128; j += blockDim.x) {
+        double sj, cj;
+        sincospi((double)j / 64.0, &sj, &cj);
+        tab[j] = make_double2(sj, cj);
+    }
+}
+
+__global__ void sincos_check_kernel(uint32_t n, uint64_t seed, double scale, double *max_err) {
+    __shared__ double2 tab[128];
+    fill_sincos_table(tab);
+    __syncthreads();
+    double worst = 0.0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        // a deterministic spread of arguments over [-scale, scale] (splitmix64 stream)
+        uint64_t z = seed + 0x9e3779b97f4a7c15ull * (i + 1);
+        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+        z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+        z ^= z >> 31;
+        const double x = ((double)(z >> 11) * 0x1.0p-53 * 2.0 - 1.0) * scale;
+        double s1, c1, s2, c2;
+        table_sincos(x, tab, &s1, &c1);
+        sincos(x, &s2, &c2);
+        worst = fmax(worst, fmax(fabs(s1 - s2), fabs(c1 - c2)));
+    }
+    for (int o = 16; o > 0; o >>= 1) worst = fmax(worst, __shfl_xor_sync(0xffffffffu, worst, o));
+    if ((threadIdx.x & 31) == 0) {
+        // non-negative doubles order like their bit patterns
+        atomicMax(reinterpret_cast<unsigned long long *>(max_err), __double_as_longlong(worst));
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Plain FP64 kernel: the reference's arithmetic, one frequency per thread.
 // ---------------------------------------------------------------------------
@@ -563,6 +636,8 @@ __global__ void __launch_bounds__(NT) plain_kernel(PlainArgs a) {
     __shared__ uint32_t s_unit;
     __shared__ double s_bp[NT / 32];
     __shared__ uint32_t s_bk[NT / 32];
+    __shared__ double2 s_tab[128];
+    fill_sincos_table(s_tab);  // made visible by the first barrier of the unit loop
     const InT *T = reinterpret_cast<const InT *>(a.t);
     const InT *Y = reinterpret_cast<const InT *>(a.y);
     const InT *DY = reinterpret_cast<const InT *>(a.dy);
@@ -595,7 +670,7 @@ __global__ void __launch_bounds__(NT) plain_kernel(PlainArgs a) {
 #pragma unroll 2
                 for (uint32_t j = 0; j < cnt; ++j) {
                     double s, c;
-                    sincos(w * s_t[j], &s, &c);
+                    table_sincos(w * s_t[j], s_tab, &s, &c);
                     const double yj = s_y[j];
                     xc += yj * c;
                     xs += yj * s;
@@ -649,7 +724,7 @@ __global__ void __launch_bounds__(NT) plain_kernel(PlainArgs a) {
                         for (uint32_t j = 0; j < cnt; ++j) {
                             const double wj = s_w[j];
                             double s, c;
-                            sincos(w * s_t[j], &s, &c);
+                            table_sincos(w * s_t[j], s_tab, &s, &c);
                             wsum += wj;
                             S += wj * s;
                             C += wj * c;
@@ -661,7 +736,7 @@ __global__ void __launch_bounds__(NT) plain_kernel(PlainArgs a) {
                         for (uint32_t j = 0; j < cnt; ++j) {
                             const double wj = s_w[j], yj = s_y[j];
                             double s, c;
-                            sincos(w * (s_t[j] - tau), &s, &c);
+                            table_sincos(w * (s_t[j] - tau), s_tab, &s, &c);
                             Y_ += wj * yj;
                             YY += wj * yj * yj;
                             Ct += wj * c;
@@ -890,6 +965,12 @@ cudaError_t plain_occupancy(int variant, int in_dtype, int out_dtype, size_t sme
     PlainArgs dummy{};
     return variant == 0 ? plain_dispatch<false>(in_dtype, out_dtype, dummy, 0, smem, 0, blocks)
                         : plain_dispatch<true>(in_dtype, out_dtype, dummy, 0, smem, 0, blocks);
+}
+
+cudaError_t launch_sincos_check(uint32_t n, uint64_t seed, double scale, double *max_err,
+                                cudaStream_t st) {
+    sincos_check_kernel<<<256, 256, 0, st>>>(n, seed, scale, max_err);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_key_decode(int dtype, const unsigned long long *keys, uint32_t n_obj,

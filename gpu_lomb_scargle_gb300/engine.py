@@ -86,6 +86,13 @@ class Engine:
         self._check(self._lib.lsgb_set_tuning(self._h, variant, freqs_per_thread, threads,
                                               min_ctas, packed, unroll))
 
+    def fp64_sincos_check(self, n: int = 1 << 22, scale: float = 1e3) -> float:
+        """Largest |difference| of the plain form's FP64 sin/cos from CUDA's sincos()."""
+        out = ctypes.c_double()
+        self._check(self._lib.lsgb_fp64_sincos_check(self._h, int(n), float(scale),
+                                                     ctypes.byref(out)))
+        return float(out.value)
+
     def set_reanchor(self, interval: int):
         self._check(self._lib.lsgb_set_reanchor(self._h, int(interval)))
 

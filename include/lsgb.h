@@ -159,6 +159,11 @@ LSGB_API void lsgb_server_destroy(lsgb_server *srv);
  * min CTAs per SM, packed, unroll), at most max_shapes of them. Returns how many exist. */
 LSGB_API int lsgb_mixed_shapes(int *out, int max_shapes);
 
+/* Self-check of the plain form's FP64 sine/cosine (Cody-Waite reduction, table of
+ * sin/cos(j pi/64), short polynomials) against CUDA's sincos() on n arguments spread
+ * over [-scale, scale]: *max_err receives the largest absolute difference. */
+LSGB_API int lsgb_fp64_sincos_check(lsgb_engine *eng, uint32_t n, double scale, double *max_err);
+
 /* Re-anchoring interval R of the mixed form's recurrence. 0 (default): every thread's
  * run of F frequencies starts from an exact anchor, so no frequency is more than F-1
  * recurrence steps from one. R > 0: anchors only at multiples of R, each thread reaching

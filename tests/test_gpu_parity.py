@@ -226,3 +226,12 @@ def test_every_compiled_mixed_shape(eng, shape):
     err = mixed_abs_err(r.pgram, ref)
     assert err < MIXED_ATOL, err
     assert check_best(r.best_idx, ref, tol=MIXED_ATOL) == []
+
+
+@pytest.mark.parametrize("scale", [3.2, 1e3, 3e5, 4e8, 5e9])
+def test_plain_fp64_sincos_against_cuda(eng, scale):
+    """The plain form's table-driven FP64 sine/cosine against CUDA's sincos(): both are
+    within about an ulp of the exact value, so they differ by a few 1e-16 at most (the
+    largest scale exercises the fallback to sincos() above 1e9 rad)."""
+    err = eng.fp64_sincos_check(1 << 22, scale)
+    assert err < 6e-16, err
