@@ -2,10 +2,11 @@
 """Throughput of the Lomb-Scargle hot path on one GB300, one JSON line on stdout.
 
 Workload (the reference's headline batch): 999 objects with log-normal observation
-counts (round(LogNormal(ln 150, 0.6)) clipped to [20, 1500], ~150k rows, seeded,
+counts (round(LogNormal(ln 150, 0.6)) clipped to [20, 1500], ~176k rows, seeded,
 synthetic), standard L-S, 1e6 angular frequencies in [1.005, 150.796). One step =
 one batch periodogram with the fused per-object argmax, mixed precision form, inputs
-resident in HBM. Metric: observation x frequency pairs per second.
+resident in HBM, replayed from a CUDA-graph plan (lsgb_plan_launch). Metric:
+observation x frequency pairs per second.
 
 Also reported on the same line:
   plain_fp64   the FP64 drop-in form on the first frequencies of the same grid;
@@ -16,7 +17,9 @@ Also reported on the same line:
   roofline     the mixed kernel's FP32-pipe ops (8 per pair) per second against the
                FP32 FMA peak measured in the same run (cuBLAS SGEMM, TF32 off);
   cpu_baseline the FP64 oracle (the reference's CPU algorithm) on all host cores;
-  clocks       nvidia-smi samples taken during the timed region.
+  clocks       nvidia-smi samples taken during the timed region;
+  serving      the continuous-batching loop on a Poisson stream (100,000 objects at
+               2,000/s, 2e5 frequencies): p50 / p99 latency and throughput.
 `--impl reference` runs the reference arm: the reference's CPU algorithm on the
 host cores (its own build when it is present, else the oracle port).
 """
@@ -251,12 +254,12 @@ def main():
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream()
 
-    def step():
-        eng.run_device(0, "mixed", t, y, None, w.offsets, w.fmin, w.df, w.n_freq, True, None, bi,
-                       bp, stream)
+    # the timed steps replay a CUDA-graph plan of the batch (one cudaGraphLaunch per step)
+    plan = eng.plan(0, "mixed", t, y, None, w.offsets, w.fmin, w.df, w.n_freq, True, None, bi, bp)
+    kernels_per_step = plan.info()[0]
 
     for _ in range(args.warmup):
-        step()
+        plan.launch(stream)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -269,17 +272,16 @@ def main():
         for i in range(args.steps):
             flush.zero_()  # L2 flush between timed steps (outside the events)
             starts[i].record(stream)
-            step()
+            plan.launch(stream)
             ends[i].record(stream)
-            kern_ms.append(eng.last_kernel_ms())
-            launches += eng.launch_info()[0]
+            kern_ms.append(plan.info(kernel_time=True)[2])
+            launches += kernels_per_step
         torch.cuda.synchronize()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     ms = float(np.mean(step_ms))
     if world > 1:
-        tt = torch.tensor([ms], dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms = float(tt.item())
+        from gpu_lomb_scargle_gb300 import shard
+        ms = shard.max_over_ranks(ms)  # the slowest rank's step time
     value = w.pairs * world / (ms / 1e3)
     best_idx = bi.cpu().numpy()
 
@@ -373,6 +375,7 @@ def main():
 
     if args.serve_objects:
         from gpu_lomb_scargle_gb300 import serve
+        plan.close()
         eng.close()
         torch.cuda.empty_cache()
         st = synth.stream(n_obj=args.serve_objects)

@@ -20,7 +20,8 @@ LSGB_SYMBOLS = ("lsgb_engine_create", "lsgb_engine_destroy", "lsgb_last_error", 
                 "lsgb_last_launch_info", "lsgb_last_kernel_time", "lsgb_mixed_shapes",
                 "lsgb_get_tuning", "lsgb_periodogram_noalloc", "lsgb_server_create",
                 "lsgb_server_submit", "lsgb_server_poll", "lsgb_server_stats", "lsgb_server_now",
-                "lsgb_server_destroy", "lsgb_set_reanchor", "lsgb_fp64_sincos_check")
+                "lsgb_server_destroy", "lsgb_set_reanchor", "lsgb_fp64_sincos_check", "lsgb_plan_create",
+                "lsgb_plan_launch", "lsgb_plan_info", "lsgb_plan_destroy")
 PYABI_SYMBOLS = ("LombScarglePy", "LombScarglePy_last_status")
 
 
@@ -93,5 +94,14 @@ def lsgb() -> ctypes.CDLL:
         lib.lsgb_set_reanchor.restype = i32
         lib.lsgb_fp64_sincos_check.argtypes = [vp, u32, dbl, c.POINTER(c.c_double)]
         lib.lsgb_fp64_sincos_check.restype = i32
+        lib.lsgb_plan_create.argtypes = common + [c.POINTER(vp)]
+        lib.lsgb_plan_create.restype = i32
+        lib.lsgb_plan_launch.argtypes = [vp, vp]
+        lib.lsgb_plan_launch.restype = i32
+        lib.lsgb_plan_info.argtypes = [vp, c.POINTER(c.c_uint32), c.POINTER(c.c_uint64),
+                                       c.POINTER(c.c_float)]
+        lib.lsgb_plan_info.restype = i32
+        lib.lsgb_plan_destroy.argtypes = [vp]
+        lib.lsgb_plan_destroy.restype = None
         lib._lsgb_typed = True
     return lib

@@ -78,6 +78,219 @@ void two_prod(double a, double b_hi, double b_lo, double &hi, double &lo) {
     hi = s;
 }
 
+// ---- one batch: plan (host), tables (upload), kernels (enqueue) ----------------------
+
+// Device buffers one batch needs besides the caller's arrays.
+struct Workspace {
+    DevBuf objs, offs, perm, rec, tile_best, counter, keys;
+    void release() {
+        DevBuf *b[] = {&objs, &offs, &perm, &rec, &tile_best, &counter, &keys};
+        for (DevBuf *x : b) x->release();
+    }
+};
+
+// Everything about a batch decided on the host.
+struct Batch {
+    bool empty = false;  // n_freq == 0: nothing to compute
+    int variant = 0, precision = 0, dtype = 0, normalize = 0;
+    const void *t = nullptr, *y = nullptr, *dy = nullptr;
+    void *pgram = nullptr, *best_power = nullptr;
+    uint32_t *best_idx = nullptr;
+    uint32_t n_obj = 0, n_freq = 0, n_tiles = 0, max_n = 0, chunk = 0;
+    uint64_t rows = 0, units = 0;
+    double fmin = 0, df = 0;
+    MixedShape shape{};
+    uint32_t reanchor = 0;
+    bool want_best = false, fold = false;
+    size_t smem = 0;
+    int grid = 0;
+    uint32_t kernels = 0;
+    std::vector<ObjInfo> objs;
+    std::vector<uint32_t> perm;
+    std::vector<uint64_t> offsets;
+};
+
+int plan_batch(Batch &b, int sms, const MixedShape *shapes, uint32_t reanchor, int variant,
+               int precision, int dtype, const void *t, const void *y, const void *dy,
+               const uint64_t *offsets, uint32_t n_obj, double fmin, double df, uint32_t n_freq,
+               int normalize, void *pgram, uint32_t *best_idx, void *best_power) {
+    if (variant != LSGB_STANDARD && variant != LSGB_GENERALIZED)
+        return fail(LSGB_ERR_INVALID, "variant %d is not LSGB_STANDARD or LSGB_GENERALIZED", variant);
+    if (precision != LSGB_PLAIN_FP64 && precision != LSGB_MIXED)
+        return fail(LSGB_ERR_INVALID, "precision %d is not LSGB_PLAIN_FP64 or LSGB_MIXED", precision);
+    if (dtype != LSGB_F32 && dtype != LSGB_F64)
+        return fail(LSGB_ERR_INVALID, "dtype %d is not LSGB_F32 or LSGB_F64", dtype);
+    if (n_obj == 0) return fail(LSGB_ERR_INVALID, "n_obj is 0");
+    if (!offsets) return fail(LSGB_ERR_INVALID, "offsets is NULL");
+    if (!t || !y) return fail(LSGB_ERR_INVALID, "t or y is NULL");
+    if (variant == LSGB_GENERALIZED && !dy)
+        return fail(LSGB_ERR_INVALID, "dy is NULL for the generalized variant");
+    if (!std::isfinite(fmin) || !std::isfinite(df))
+        return fail(LSGB_ERR_INVALID, "fmin/df must be finite");
+    if (offsets[0] != 0) return fail(LSGB_ERR_INVALID, "offsets[0] must be 0");
+    b.objs.assign(n_obj, ObjInfo{});
+    uint32_t max_n = 0;
+    for (uint32_t o = 0; o < n_obj; ++o) {
+        if (offsets[o + 1] <= offsets[o])
+            return fail(LSGB_ERR_INVALID, "object %u has no observations (offsets must increase)", o);
+        const uint64_t n = offsets[o + 1] - offsets[o];
+        if (n > 0xffffffffull) return fail(LSGB_ERR_INVALID, "object %u has more than 2^32-1 rows", o);
+        b.objs[o].row0 = offsets[o];
+        b.objs[o].n = (uint32_t)n;
+        max_n = std::max<uint32_t>(max_n, (uint32_t)n);
+    }
+    b.empty = n_freq == 0;
+    if (b.empty) return LSGB_OK;  // nothing to compute or write
+    b.variant = variant;
+    b.precision = precision;
+    b.dtype = dtype;
+    b.normalize = normalize;
+    b.t = t;
+    b.y = y;
+    b.dy = dy;
+    b.pgram = pgram;
+    b.best_idx = best_idx;
+    b.best_power = best_power;
+    b.n_obj = n_obj;
+    b.n_freq = n_freq;
+    b.fmin = fmin;
+    b.df = df;
+    b.max_n = max_n;
+    b.rows = offsets[n_obj];
+    b.offsets.assign(offsets, offsets + n_obj + 1);
+    // Work order: largest objects first (longest-processing-time first), ties by index.
+    b.perm.resize(n_obj);
+    std::iota(b.perm.begin(), b.perm.end(), 0u);
+    std::stable_sort(b.perm.begin(), b.perm.end(),
+                     [&](uint32_t x, uint32_t z) { return b.objs[x].n > b.objs[z].n; });
+    const bool mixed = precision == LSGB_MIXED;
+    b.shape = shapes[variant];
+    b.reanchor = mixed ? reanchor : 0;
+    const uint32_t tile_freqs = mixed ? (uint32_t)(b.shape.f * b.shape.nt) : (uint32_t)kPlainThreads;
+    const uint64_t n_tiles64 = (n_freq + (uint64_t)tile_freqs - 1) / tile_freqs;
+    b.units = n_tiles64 * n_obj;
+    if (b.units >= 0xffffffffull)
+        return fail(LSGB_ERR_INVALID, "%llu work units exceed the 2^32 queue; split the batch",
+                    (unsigned long long)b.units);
+    b.n_tiles = (uint32_t)n_tiles64;
+    b.want_best = best_idx || best_power;
+    int occ = 0;
+    if (mixed) {
+        const uint32_t rec_bytes = (uint32_t)mixed_rec_bytes(b.shape);
+        b.chunk = std::min<uint32_t>(max_n, kMixedSmemMax / rec_bytes);
+        // objects longer than one chunk sum in two levels (chunk sums folded in smem)
+        b.fold = max_n > b.chunk;
+        b.smem = (size_t)rec_bytes * b.chunk + (b.fold ? mixed_fold_bytes(variant, b.shape) : 0);
+        LSGB_CUDA(mixed_occupancy(variant, dtype, b.shape, b.smem, &occ));
+        if (occ < 1) return fail(LSGB_ERR_CUDA, "mixed kernel does not fit on an SM (smem %zu)", b.smem);
+    } else {
+        b.chunk = std::min<uint32_t>(max_n, kPlainChunkMax);
+        b.smem = sizeof(double) * b.chunk * (variant == LSGB_GENERALIZED ? 3 : 2);
+        LSGB_CUDA(plain_occupancy(variant, dtype, dtype, b.smem, &occ));
+        if (occ < 1) return fail(LSGB_ERR_CUDA, "plain kernel does not fit on an SM (smem %zu)", b.smem);
+    }
+    b.grid = (int)std::min<uint64_t>((uint64_t)sms * occ, b.units);
+    return LSGB_OK;
+}
+
+// Sizes the workspace and copies the per-object tables (stream-ordered).
+int upload_tables(const Batch &b, Workspace &ws, cudaStream_t st) {
+    const bool mixed = b.precision == LSGB_MIXED;
+    LSGB_CUDA(ws.objs.ensure(sizeof(ObjInfo) * b.n_obj));
+    LSGB_CUDA(ws.offs.ensure(sizeof(uint64_t) * (b.n_obj + 1)));
+    LSGB_CUDA(ws.perm.ensure(sizeof(uint32_t) * b.n_obj));
+    LSGB_CUDA(ws.counter.ensure(sizeof(uint32_t)));
+    if (b.want_best && !mixed) LSGB_CUDA(ws.tile_best.ensure(sizeof(TileBest) * b.units));
+    if (b.want_best && mixed) LSGB_CUDA(ws.keys.ensure(sizeof(unsigned long long) * b.n_obj));
+    if (mixed) LSGB_CUDA(ws.rec.ensure(sizeof(ObsRec) * b.rows));
+    LSGB_CUDA(cudaMemcpyAsync(ws.objs.p, b.objs.data(), sizeof(ObjInfo) * b.n_obj,
+                              cudaMemcpyHostToDevice, st));
+    LSGB_CUDA(cudaMemcpyAsync(ws.offs.p, b.offsets.data(), sizeof(uint64_t) * (b.n_obj + 1),
+                              cudaMemcpyHostToDevice, st));
+    LSGB_CUDA(cudaMemcpyAsync(ws.perm.p, b.perm.data(), sizeof(uint32_t) * b.n_obj,
+                              cudaMemcpyHostToDevice, st));
+    return LSGB_OK;
+}
+
+// Records `ev` on `st`; while `st` is being captured the record becomes an event node
+// of the graph (a plain record there would only mark a capture dependency).
+cudaError_t record(cudaEvent_t ev, cudaStream_t st, bool capturing) {
+    return capturing ? cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal)
+                     : cudaEventRecord(ev, st);
+}
+
+// The device work of a batch: memsets and kernels only, so it can be captured in a graph.
+// ev0/ev1 (may be null) are recorded around the main kernel.
+int enqueue_batch(Batch &b, Workspace &ws, cudaStream_t st, cudaEvent_t ev0, cudaEvent_t ev1,
+                  bool capturing = false) {
+    const bool mixed = b.precision == LSGB_MIXED;
+    ObjInfo *d_objs = (ObjInfo *)ws.objs.p;
+    uint32_t kernels = 0;
+    LSGB_CUDA(cudaMemsetAsync(ws.counter.p, 0, sizeof(uint32_t), st));
+    if (b.want_best && mixed)
+        LSGB_CUDA(cudaMemsetAsync(ws.keys.p, 0, sizeof(unsigned long long) * b.n_obj, st));
+    LSGB_CUDA(launch_stats(b.variant, mixed ? 1 : 0, b.dtype, b.normalize, b.y, b.dy, d_objs,
+                           b.n_obj, st));
+    ++kernels;
+    if (mixed) {
+        GridTurns g;
+        two_prod(b.fmin, kInv2PiHi, kInv2PiLo, g.f0_hi, g.f0_lo);
+        two_prod(b.df, kInv2PiHi, kInv2PiLo, g.df_hi, g.df_lo);
+        LSGB_CUDA(launch_records(b.variant, b.dtype, b.t, b.y, b.dy, (const uint64_t *)ws.offs.p,
+                                 b.n_obj, d_objs, b.rows, g, (ObsRec *)ws.rec.p, st));
+        ++kernels;
+        MixedArgs a{};
+        a.rec = (const ObsRec *)ws.rec.p;
+        a.objs = d_objs;
+        a.perm = (const uint32_t *)ws.perm.p;
+        a.n_obj = b.n_obj;
+        a.n_tiles = b.n_tiles;
+        a.n_freq = b.n_freq;
+        a.chunk = b.chunk;
+        a.counter = (uint32_t *)ws.counter.p;
+        a.pgram = b.pgram;
+        a.tile_best = nullptr;
+        a.best_key = b.want_best ? (unsigned long long *)ws.keys.p : nullptr;
+        a.reanchor = b.reanchor;
+        a.fold = b.fold ? 1u : 0u;
+        if (ev0) LSGB_CUDA(record(ev0, st, capturing));
+        LSGB_CUDA(launch_mixed(b.variant, b.dtype, b.shape, a, b.grid, b.smem, st));
+        if (ev1) LSGB_CUDA(record(ev1, st, capturing));
+        ++kernels;
+    } else {
+        PlainArgs a{};
+        a.t = b.t;
+        a.y = b.y;
+        a.dy = b.dy;
+        a.objs = d_objs;
+        a.perm = (const uint32_t *)ws.perm.p;
+        a.n_obj = b.n_obj;
+        a.n_tiles = b.n_tiles;
+        a.n_freq = b.n_freq;
+        a.chunk = b.chunk;
+        a.fmin = b.fmin;
+        a.df = b.df;
+        a.counter = (uint32_t *)ws.counter.p;
+        a.pgram = b.pgram;
+        a.tile_best = b.want_best ? (TileBest *)ws.tile_best.p : nullptr;
+        if (ev0) LSGB_CUDA(record(ev0, st, capturing));
+        LSGB_CUDA(launch_plain(b.variant, b.dtype, b.dtype, a, b.grid, b.smem, st));
+        if (ev1) LSGB_CUDA(record(ev1, st, capturing));
+        ++kernels;
+    }
+    if (b.want_best && mixed) {
+        LSGB_CUDA(launch_key_decode(b.dtype, (const unsigned long long *)ws.keys.p, b.n_obj,
+                                    b.best_idx, b.best_power, st));
+        ++kernels;
+    } else if (b.want_best) {
+        LSGB_CUDA(launch_best_reduce(b.dtype, (const TileBest *)ws.tile_best.p, b.n_obj, b.n_tiles,
+                                     b.best_idx, b.best_power, st));
+        ++kernels;
+    }
+    b.kernels = kernels;
+    return LSGB_OK;
+}
+
 }  // namespace
 
 namespace lsgb {
@@ -89,7 +302,8 @@ struct lsgb_engine {
     int device = 0;
     int sms = 0;
     cudaStream_t stream = nullptr;  // host-buffer API stream
-    DevBuf objs, offs, perm, rec, tile_best, counter, keys;
+    cudaStream_t d2h = nullptr;     // host-buffer API: periodogram copies overlapping compute
+    Workspace ws;
     DevBuf in_t, in_y, in_dy, out_pg, out_idx, out_p;
     MixedShape shape[2] = {{12, 256, 2, 1, 0}, {8, 256, 2, 1, 0}};
     uint32_t last_kernels = 0;
@@ -97,6 +311,18 @@ struct lsgb_engine {
     cudaEvent_t ev_main0 = nullptr, ev_main1 = nullptr;  // around the last main-kernel launch
     bool ev_valid = false;
     uint32_t reanchor = 0;  // mixed form: 0 = anchor at each thread's frequency run
+};
+
+// A batch whose device work is captured once in a CUDA graph and replayed.
+struct lsgb_plan {
+    int device = 0;
+    Workspace ws;
+    Batch b;
+    cudaStream_t cap = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool launched = false;
 };
 
 extern "C" {
@@ -120,7 +346,7 @@ LSGB_API int lsgb_engine_create(int device, lsgb_engine **out) {
     eng->device = device;
     cudaError_t e2 = cudaDeviceGetAttribute(&eng->sms, cudaDevAttrMultiProcessorCount, device);
     if (e2 == cudaSuccess) e2 = cudaStreamCreateWithFlags(&eng->stream, cudaStreamNonBlocking);
-    if (e2 == cudaSuccess) e2 = eng->counter.ensure(256);
+    if (e2 == cudaSuccess) e2 = cudaStreamCreateWithFlags(&eng->d2h, cudaStreamNonBlocking);
     if (e2 == cudaSuccess) e2 = cudaEventCreate(&eng->ev_main0);
     if (e2 == cudaSuccess) e2 = cudaEventCreate(&eng->ev_main1);
     if (e2 != cudaSuccess) {
@@ -135,11 +361,11 @@ LSGB_API void lsgb_engine_destroy(lsgb_engine *eng) {
     if (!eng) return;
     cudaSetDevice(eng->device);
     if (eng->stream) cudaStreamSynchronize(eng->stream);
-    DevBuf *bufs[] = {&eng->objs,   &eng->offs,  &eng->perm,    &eng->rec,
-                      &eng->tile_best, &eng->counter, &eng->keys, &eng->in_t, &eng->in_y,
-                      &eng->in_dy,  &eng->out_pg, &eng->out_idx, &eng->out_p};
+    eng->ws.release();
+    DevBuf *bufs[] = {&eng->in_t, &eng->in_y, &eng->in_dy, &eng->out_pg, &eng->out_idx, &eng->out_p};
     for (DevBuf *b : bufs) b->release();
     if (eng->stream) cudaStreamDestroy(eng->stream);
+    if (eng->d2h) cudaStreamDestroy(eng->d2h);
     if (eng->ev_main0) cudaEventDestroy(eng->ev_main0);
     if (eng->ev_main1) cudaEventDestroy(eng->ev_main1);
     delete eng;
@@ -219,152 +445,100 @@ LSGB_API int lsgb_periodogram_device(lsgb_engine *eng, int variant, int precisio
                                      double df, uint32_t n_freq, int normalize, void *pgram,
                                      uint32_t *best_idx, void *best_power, void *stream_) {
     if (!eng) return fail(LSGB_ERR_INVALID, "engine is NULL");
-    if (variant != LSGB_STANDARD && variant != LSGB_GENERALIZED)
-        return fail(LSGB_ERR_INVALID, "variant %d is not LSGB_STANDARD or LSGB_GENERALIZED", variant);
-    if (precision != LSGB_PLAIN_FP64 && precision != LSGB_MIXED)
-        return fail(LSGB_ERR_INVALID, "precision %d is not LSGB_PLAIN_FP64 or LSGB_MIXED", precision);
-    if (dtype != LSGB_F32 && dtype != LSGB_F64)
-        return fail(LSGB_ERR_INVALID, "dtype %d is not LSGB_F32 or LSGB_F64", dtype);
-    if (n_obj == 0) return fail(LSGB_ERR_INVALID, "n_obj is 0");
-    if (!offsets) return fail(LSGB_ERR_INVALID, "offsets is NULL");
-    if (!t || !y) return fail(LSGB_ERR_INVALID, "t or y is NULL");
-    if (variant == LSGB_GENERALIZED && !dy)
-        return fail(LSGB_ERR_INVALID, "dy is NULL for the generalized variant");
-    if (!std::isfinite(fmin) || !std::isfinite(df))
-        return fail(LSGB_ERR_INVALID, "fmin/df must be finite");
-    if (offsets[0] != 0) return fail(LSGB_ERR_INVALID, "offsets[0] must be 0");
-    uint32_t max_n = 0;
-    std::vector<ObjInfo> h_objs(n_obj);
-    for (uint32_t o = 0; o < n_obj; ++o) {
-        if (offsets[o + 1] <= offsets[o])
-            return fail(LSGB_ERR_INVALID, "object %u has no observations (offsets must increase)", o);
-        const uint64_t n = offsets[o + 1] - offsets[o];
-        if (n > 0xffffffffull) return fail(LSGB_ERR_INVALID, "object %u has more than 2^32-1 rows", o);
-        ObjInfo ob{};
-        ob.row0 = offsets[o];
-        ob.n = (uint32_t)n;
-        h_objs[o] = ob;
-        max_n = std::max<uint32_t>(max_n, (uint32_t)n);
-    }
     eng->last_kernels = 0;
     eng->last_units = 0;
-    if (n_freq == 0) return LSGB_OK;  // nothing to compute or write
-    const uint64_t rows = offsets[n_obj];
     cudaStream_t st = (cudaStream_t)stream_;
     LSGB_CUDA(cudaSetDevice(eng->device));
+    Batch b;
+    int rc = plan_batch(b, eng->sms, eng->shape, eng->reanchor, variant, precision, dtype, t, y, dy,
+                        offsets, n_obj, fmin, df, n_freq, normalize, pgram, best_idx, best_power);
+    if (rc != LSGB_OK || b.empty) return rc;
+    rc = upload_tables(b, eng->ws, st);
+    if (rc != LSGB_OK) return rc;
+    rc = enqueue_batch(b, eng->ws, st, eng->ev_main0, eng->ev_main1);
+    if (rc != LSGB_OK) return rc;
+    eng->ev_valid = true;
+    eng->last_kernels = b.kernels;
+    eng->last_units = b.units;
+    return LSGB_OK;
+}
 
-    // Work order: largest objects first (longest-processing-time first), ties by index.
-    std::vector<uint32_t> h_perm(n_obj);
-    std::iota(h_perm.begin(), h_perm.end(), 0u);
-    std::stable_sort(h_perm.begin(), h_perm.end(),
-                     [&](uint32_t a, uint32_t b) { return h_objs[a].n > h_objs[b].n; });
+LSGB_API void lsgb_plan_destroy(lsgb_plan *p) {
+    if (!p) return;
+    cudaSetDevice(p->device);
+    if (p->cap) cudaStreamSynchronize(p->cap);
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    if (p->ev0) cudaEventDestroy(p->ev0);
+    if (p->ev1) cudaEventDestroy(p->ev1);
+    if (p->cap) cudaStreamDestroy(p->cap);
+    p->ws.release();
+    delete p;
+}
 
-    const bool mixed = precision == LSGB_MIXED;
-    const MixedShape shape = eng->shape[variant];
-    const uint32_t tile_freqs = mixed ? (uint32_t)(shape.f * shape.nt) : (uint32_t)kPlainThreads;
-    const uint64_t n_tiles64 = (n_freq + (uint64_t)tile_freqs - 1) / tile_freqs;
-    const uint64_t n_units64 = n_tiles64 * n_obj;
-    if (n_units64 >= 0xffffffffull)
-        return fail(LSGB_ERR_INVALID, "%llu work units exceed the 2^32 queue; split the batch",
-                    (unsigned long long)n_units64);
-    const uint32_t n_tiles = (uint32_t)n_tiles64;
-    const bool want_best = best_idx || best_power;
-
-    LSGB_CUDA(eng->objs.ensure(sizeof(ObjInfo) * n_obj));
-    LSGB_CUDA(eng->offs.ensure(sizeof(uint64_t) * (n_obj + 1)));
-    LSGB_CUDA(eng->perm.ensure(sizeof(uint32_t) * n_obj));
-    if (want_best && !mixed) LSGB_CUDA(eng->tile_best.ensure(sizeof(TileBest) * n_units64));
-    if (want_best && mixed) {
-        LSGB_CUDA(eng->keys.ensure(sizeof(unsigned long long) * n_obj));
-        LSGB_CUDA(cudaMemsetAsync(eng->keys.p, 0, sizeof(unsigned long long) * n_obj, st));
+LSGB_API int lsgb_plan_create(lsgb_engine *eng, int variant, int precision, int dtype,
+                              const void *t, const void *y, const void *dy,
+                              const uint64_t *offsets, uint32_t n_obj, double fmin, double df,
+                              uint32_t n_freq, int normalize, void *pgram, uint32_t *best_idx,
+                              void *best_power, lsgb_plan **out) {
+    if (!eng || !out) return fail(LSGB_ERR_INVALID, "lsgb_plan_create: NULL engine or out");
+    *out = nullptr;
+    if (n_freq == 0) return fail(LSGB_ERR_INVALID, "lsgb_plan_create: n_freq is 0");
+    LSGB_CUDA(cudaSetDevice(eng->device));
+    lsgb_plan *p = new lsgb_plan();
+    p->device = eng->device;
+    int rc = plan_batch(p->b, eng->sms, eng->shape, eng->reanchor, variant, precision, dtype, t, y,
+                        dy, offsets, n_obj, fmin, df, n_freq, normalize, pgram, best_idx,
+                        best_power);
+    cudaError_t e = cudaSuccess;
+    if (rc == LSGB_OK) {
+        e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreate(&p->ev0);
+        if (e == cudaSuccess) e = cudaEventCreate(&p->ev1);
+        if (e != cudaSuccess) rc = fail(LSGB_ERR_CUDA, "plan set-up: %s", cudaGetErrorString(e));
     }
-    if (mixed) LSGB_CUDA(eng->rec.ensure(sizeof(ObsRec) * rows));
-    LSGB_CUDA(cudaMemcpyAsync(eng->objs.p, h_objs.data(), sizeof(ObjInfo) * n_obj,
-                              cudaMemcpyHostToDevice, st));
-    LSGB_CUDA(cudaMemcpyAsync(eng->offs.p, offsets, sizeof(uint64_t) * (n_obj + 1),
-                              cudaMemcpyHostToDevice, st));
-    LSGB_CUDA(cudaMemcpyAsync(eng->perm.p, h_perm.data(), sizeof(uint32_t) * n_obj,
-                              cudaMemcpyHostToDevice, st));
-    LSGB_CUDA(cudaMemsetAsync(eng->counter.p, 0, sizeof(uint32_t), st));
+    if (rc == LSGB_OK) rc = upload_tables(p->b, p->ws, p->cap);
+    if (rc == LSGB_OK && (e = cudaStreamSynchronize(p->cap)) != cudaSuccess)
+        rc = fail(LSGB_ERR_CUDA, "plan upload: %s", cudaGetErrorString(e));
+    if (rc == LSGB_OK) {
+        // relaxed: the launch helpers set kernel attributes (not stream work) while capturing
+        e = cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeRelaxed);
+        if (e != cudaSuccess) rc = fail(LSGB_ERR_CUDA, "begin capture: %s", cudaGetErrorString(e));
+        if (rc == LSGB_OK) {
+            const int rc2 = enqueue_batch(p->b, p->ws, p->cap, p->ev0, p->ev1, true);
+            e = cudaStreamEndCapture(p->cap, &p->graph);
+            if (rc2 != LSGB_OK) rc = rc2;
+            else if (e != cudaSuccess)
+                rc = fail(LSGB_ERR_CUDA, "end capture: %s", cudaGetErrorString(e));
+        }
+    }
+    if (rc == LSGB_OK && (e = cudaGraphInstantiate(&p->exec, p->graph, 0)) != cudaSuccess)
+        rc = fail(LSGB_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    if (rc != LSGB_OK) {
+        lsgb_plan_destroy(p);
+        return rc;
+    }
+    *out = p;
+    return LSGB_OK;
+}
 
-    ObjInfo *d_objs = (ObjInfo *)eng->objs.p;
-    uint32_t kernels = 0;
-    LSGB_CUDA(launch_stats(variant, mixed ? 1 : 0, dtype, normalize, y, dy, d_objs, n_obj, st));
-    ++kernels;
-    if (mixed) {
-        GridTurns g;
-        two_prod(fmin, kInv2PiHi, kInv2PiLo, g.f0_hi, g.f0_lo);
-        two_prod(df, kInv2PiHi, kInv2PiLo, g.df_hi, g.df_lo);
-        LSGB_CUDA(launch_records(variant, dtype, t, y, dy, (const uint64_t *)eng->offs.p, n_obj,
-                                 d_objs, rows, g, (ObsRec *)eng->rec.p, st));
-        ++kernels;
-        const uint32_t rec_bytes = (uint32_t)mixed_rec_bytes(shape);
-        const uint32_t chunk = std::min<uint32_t>(max_n, kMixedSmemMax / rec_bytes);
-        // objects longer than one chunk sum in two levels (chunk sums folded in smem)
-        const bool fold = max_n > chunk;
-        const size_t smem = (size_t)rec_bytes * chunk + (fold ? mixed_fold_bytes(variant, shape) : 0);
-        int occ = 0;
-        LSGB_CUDA(mixed_occupancy(variant, dtype, shape, smem, &occ));
-        if (occ < 1) return fail(LSGB_ERR_CUDA, "mixed kernel does not fit on an SM (smem %zu)", smem);
-        MixedArgs a{};
-        a.rec = (const ObsRec *)eng->rec.p;
-        a.objs = d_objs;
-        a.perm = (const uint32_t *)eng->perm.p;
-        a.n_obj = n_obj;
-        a.n_tiles = n_tiles;
-        a.n_freq = n_freq;
-        a.chunk = chunk;
-        a.counter = (uint32_t *)eng->counter.p;
-        a.pgram = pgram;
-        a.tile_best = nullptr;
-        a.best_key = want_best ? (unsigned long long *)eng->keys.p : nullptr;
-        a.reanchor = eng->reanchor;
-        a.fold = fold ? 1u : 0u;
-        const int grid = (int)std::min<uint64_t>((uint64_t)eng->sms * occ, n_units64);
-        LSGB_CUDA(cudaEventRecord(eng->ev_main0, st));
-        LSGB_CUDA(launch_mixed(variant, dtype, shape, a, grid, smem, st));
-        LSGB_CUDA(cudaEventRecord(eng->ev_main1, st));
-        eng->ev_valid = true;
-        ++kernels;
-    } else {
-        const uint32_t chunk = std::min<uint32_t>(max_n, kPlainChunkMax);
-        const size_t smem = sizeof(double) * chunk * (variant == LSGB_GENERALIZED ? 3 : 2);
-        int occ = 0;
-        LSGB_CUDA(plain_occupancy(variant, dtype, dtype, smem, &occ));
-        if (occ < 1) return fail(LSGB_ERR_CUDA, "plain kernel does not fit on an SM (smem %zu)", smem);
-        PlainArgs a{};
-        a.t = t;
-        a.y = y;
-        a.dy = dy;
-        a.objs = d_objs;
-        a.perm = (const uint32_t *)eng->perm.p;
-        a.n_obj = n_obj;
-        a.n_tiles = n_tiles;
-        a.n_freq = n_freq;
-        a.chunk = chunk;
-        a.fmin = fmin;
-        a.df = df;
-        a.counter = (uint32_t *)eng->counter.p;
-        a.pgram = pgram;
-        a.tile_best = want_best ? (TileBest *)eng->tile_best.p : nullptr;
-        const int grid = (int)std::min<uint64_t>((uint64_t)eng->sms * occ, n_units64);
-        LSGB_CUDA(cudaEventRecord(eng->ev_main0, st));
-        LSGB_CUDA(launch_plain(variant, dtype, dtype, a, grid, smem, st));
-        LSGB_CUDA(cudaEventRecord(eng->ev_main1, st));
-        eng->ev_valid = true;
-        ++kernels;
+LSGB_API int lsgb_plan_launch(lsgb_plan *p, void *stream) {
+    if (!p) return fail(LSGB_ERR_INVALID, "lsgb_plan_launch: plan is NULL");
+    LSGB_CUDA(cudaSetDevice(p->device));
+    LSGB_CUDA(cudaGraphLaunch(p->exec, (cudaStream_t)stream));
+    p->launched = true;
+    return LSGB_OK;
+}
+
+LSGB_API int lsgb_plan_info(lsgb_plan *p, uint32_t *kernels, uint64_t *units, float *last_kernel_ms) {
+    if (!p) return fail(LSGB_ERR_INVALID, "lsgb_plan_info: plan is NULL");
+    if (kernels) *kernels = p->b.kernels;
+    if (units) *units = p->b.units;
+    if (last_kernel_ms) {
+        if (!p->launched) return fail(LSGB_ERR_INVALID, "lsgb_plan_info: plan never launched");
+        LSGB_CUDA(cudaEventSynchronize(p->ev1));
+        LSGB_CUDA(cudaEventElapsedTime(last_kernel_ms, p->ev0, p->ev1));
     }
-    if (want_best && mixed) {
-        LSGB_CUDA(launch_key_decode(dtype, (const unsigned long long *)eng->keys.p, n_obj, best_idx,
-                                    best_power, st));
-        ++kernels;
-    } else if (want_best) {
-        LSGB_CUDA(launch_best_reduce(dtype, (const TileBest *)eng->tile_best.p, n_obj, n_tiles,
-                                     best_idx, best_power, st));
-        ++kernels;
-    }
-    eng->last_kernels = kernels;
-    eng->last_units = n_units64;
     return LSGB_OK;
 }
 
@@ -408,6 +582,76 @@ LSGB_API int lsgb_periodogram_host(lsgb_engine *eng, int variant, int precision,
     if (best_power) {
         LSGB_CUDA(eng->out_p.ensure(es * n_obj));
         d_p = eng->out_p.p;
+    }
+    // A large periodogram goes out in object chunks: every chunk's computation is queued
+    // first, then each chunk is copied to the host on a second stream as soon as it is
+    // done, so the copy of chunk c overlaps the computation of chunks c+1.. (the result
+    // of an object does not depend on the batch it is computed in).
+    const size_t kChunkBytes = size_t(512) << 20;
+    const uint32_t n_chunks =
+        (d_pg && n_freq && es * pg_elems > kChunkBytes && n_obj >= 2)
+            ? (uint32_t)std::min<uint64_t>({8ull, n_obj, (es * pg_elems + kChunkBytes - 1) / kChunkBytes})
+            : 1u;
+    if (n_chunks > 1) {
+        std::vector<uint32_t> cut{0};
+        for (uint32_t c = 1; c < n_chunks; ++c) {  // equal rows per chunk, at object boundaries
+            const uint64_t target = rows * c / n_chunks;
+            uint32_t o = (uint32_t)(std::lower_bound(offsets, offsets + n_obj + 1, target) - offsets);
+            o = std::max<uint32_t>(o, cut.back() + 1);
+            if (o < n_obj) cut.push_back(o);
+        }
+        cut.push_back(n_obj);
+        // size the workspace for the whole batch up front: growing it between chunks would
+        // free memory still in use by queued kernels (cudaFree synchronizes the device)
+        {
+            const uint64_t max_tiles = (n_freq + 255) / 256;  // the smallest tile of any form
+            LSGB_CUDA(eng->ws.objs.ensure(sizeof(ObjInfo) * n_obj));
+            LSGB_CUDA(eng->ws.offs.ensure(sizeof(uint64_t) * (n_obj + 1)));
+            LSGB_CUDA(eng->ws.perm.ensure(sizeof(uint32_t) * n_obj));
+            LSGB_CUDA(eng->ws.counter.ensure(sizeof(uint32_t)));
+            LSGB_CUDA(eng->ws.keys.ensure(sizeof(unsigned long long) * n_obj));
+            if (precision == LSGB_MIXED) LSGB_CUDA(eng->ws.rec.ensure(sizeof(ObsRec) * rows));
+            else if (best_idx || best_power)
+                LSGB_CUDA(eng->ws.tile_best.ensure(sizeof(TileBest) * max_tiles * n_obj));
+        }
+        std::vector<cudaEvent_t> ev(cut.size() - 1, nullptr);
+        int rc = LSGB_OK;
+        for (size_t c = 0; c + 1 < cut.size() && rc == LSGB_OK; ++c) {
+            const uint32_t o0 = cut[c], o1 = cut[c + 1];
+            const uint64_t r0 = offsets[o0];
+            std::vector<uint64_t> offs_c(offsets + o0, offsets + o1 + 1);
+            for (auto &v : offs_c) v -= r0;
+            rc = lsgb_periodogram_device(
+                eng, variant, precision, dtype, (const char *)eng->in_t.p + es * r0,
+                (const char *)eng->in_y.p + es * r0, d_dy ? (const char *)d_dy + es * r0 : nullptr,
+                offs_c.data(), o1 - o0, fmin, df, n_freq, normalize,
+                (char *)d_pg + es * (uint64_t)o0 * n_freq, d_idx ? d_idx + o0 : nullptr,
+                d_p ? (char *)d_p + es * o0 : nullptr, (void *)st);
+            if (rc == LSGB_OK) {
+                cudaError_t e = cudaEventCreateWithFlags(&ev[c], cudaEventDisableTiming);
+                if (e == cudaSuccess) e = cudaEventRecord(ev[c], st);
+                if (e != cudaSuccess) rc = fail(LSGB_ERR_CUDA, "chunk event: %s", cudaGetErrorString(e));
+            }
+        }
+        for (size_t c = 0; c + 1 < cut.size() && rc == LSGB_OK; ++c) {
+            const uint64_t off = es * (uint64_t)cut[c] * n_freq;
+            const uint64_t bytes = es * (uint64_t)(cut[c + 1] - cut[c]) * n_freq;
+            cudaError_t e = cudaStreamWaitEvent(eng->d2h, ev[c], 0);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync((char *)pgram + off, (const char *)d_pg + off, bytes,
+                                    cudaMemcpyDeviceToHost, eng->d2h);
+            if (e != cudaSuccess) rc = fail(LSGB_ERR_CUDA, "periodogram copy: %s", cudaGetErrorString(e));
+        }
+        cudaStreamSynchronize(st);
+        cudaStreamSynchronize(eng->d2h);
+        for (cudaEvent_t x : ev)
+            if (x) cudaEventDestroy(x);
+        if (rc != LSGB_OK) return rc;
+        if (d_idx)
+            LSGB_CUDA(cudaMemcpyAsync(best_idx, d_idx, sizeof(uint32_t) * n_obj, cudaMemcpyDeviceToHost, st));
+        if (d_p) LSGB_CUDA(cudaMemcpyAsync(best_power, d_p, es * n_obj, cudaMemcpyDeviceToHost, st));
+        LSGB_CUDA(cudaStreamSynchronize(st));
+        return LSGB_OK;
     }
     int rc = lsgb_periodogram_device(eng, variant, precision, dtype, eng->in_t.p, eng->in_y.p, d_dy,
                                      offsets, n_obj, fmin, df, n_freq, normalize, d_pg, d_idx, d_p,

@@ -135,6 +135,12 @@ class Engine:
             int(n_freq), int(bool(normalize)), ptr(pgram), ptr(best_idx), ptr(best_power), st)
         self._check(rc)
 
+    def plan(self, variant, precision, t, y, dy, offsets, fmin, df, n_freq, normalize=True,
+             pgram=None, best_idx=None, best_power=None) -> "Plan":
+        """A CUDA-graph plan of run_device with these (CUDA tensor) arguments."""
+        return Plan(self, variant, precision, t, y, dy, offsets, fmin, df, n_freq, normalize,
+                    pgram, best_idx, best_power)
+
     # ---- host-buffer call -----------------------------------------------------
     def run_host(self, variant, precision, t, y, dy, offsets, fmin, df, n_freq, normalize=True,
                  want_pgram=False, out_pgram=None, out_idx=None, out_power=None) -> Result:
@@ -156,6 +162,56 @@ class Engine:
             int(n_freq), int(bool(normalize)), vp(pg), vp(idx), vp(pw))
         self._check(rc)
         return Result(idx, pw, pg)
+
+
+class Plan:
+    """One batch shape captured in a CUDA graph (lsgb_plan_*); keeps its tensors alive."""
+
+    def __init__(self, eng, variant, precision, t, y, dy, offsets, fmin, df, n_freq, normalize,
+                 pgram, best_idx, best_power):
+        import torch
+
+        if t.dtype == torch.float32:
+            code = F32
+        elif t.dtype == torch.float64:
+            code = F64
+        else:
+            raise TypeError("t must be float32 or float64")
+        self._eng = eng
+        self._keep = (t, y, dy, pgram, best_idx, best_power)
+        offs = np.ascontiguousarray(offsets, dtype=np.uint64)
+        ptr = lambda x: ctypes.c_void_p(x.data_ptr()) if x is not None else None
+        h = ctypes.c_void_p()
+        eng._check(eng._lib.lsgb_plan_create(
+            eng._h, int(variant), _precision(precision), code, ptr(t), ptr(y), ptr(dy),
+            offs.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), offs.size - 1, float(fmin),
+            float(df), int(n_freq), int(bool(normalize)), ptr(pgram), ptr(best_idx),
+            ptr(best_power), ctypes.byref(h)))
+        self._h = h
+
+    def launch(self, stream=None):
+        import torch
+        st = stream if stream is not None else torch.cuda.current_stream()
+        self._eng._check(self._eng._lib.lsgb_plan_launch(self._h, ctypes.c_void_p(st.cuda_stream)))
+
+    def info(self, kernel_time=False):
+        k = ctypes.c_uint32()
+        u = ctypes.c_uint64()
+        ms = ctypes.c_float()
+        self._eng._check(self._eng._lib.lsgb_plan_info(self._h, ctypes.byref(k), ctypes.byref(u),
+                                                       ctypes.byref(ms) if kernel_time else None))
+        return int(k.value), int(u.value), (float(ms.value) if kernel_time else None)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._eng._lib.lsgb_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def mixed_shapes():

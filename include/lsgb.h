@@ -88,6 +88,29 @@ LSGB_API int lsgb_periodogram_host(lsgb_engine *eng, int variant, int precision,
                                    uint32_t n_freq, int normalize, void *pgram, uint32_t *best_idx,
                                    void *best_power);
 
+/* ---- execution plans: one batch shape, captured once in a CUDA graph ----
+ * lsgb_plan_create plans a batch exactly as lsgb_periodogram_device would (same
+ * arguments; device pointers are fixed into the plan), uploads its per-object tables
+ * once, and captures the kernel sequence (queue reset, statistics, records,
+ * periodogram, argmax) in a CUDA graph. lsgb_plan_launch replays it on any stream
+ * with one cudaGraphLaunch: the caller may rewrite the contents of t / y / dy
+ * between launches, not their sizes or addresses. A plan owns its scratch buffers,
+ * so plans and the engine's direct calls do not share state; two launches of one
+ * plan must not overlap on the GPU. Takes the engine's current shape and
+ * re-anchoring setting. No counterpart in the reference. */
+typedef struct lsgb_plan lsgb_plan;
+LSGB_API int lsgb_plan_create(lsgb_engine *eng, int variant, int precision, int dtype,
+                              const void *t, const void *y, const void *dy,
+                              const uint64_t *offsets_host, uint32_t n_obj, double fmin, double df,
+                              uint32_t n_freq, int normalize, void *pgram, uint32_t *best_idx,
+                              void *best_power, lsgb_plan **out);
+LSGB_API int lsgb_plan_launch(lsgb_plan *plan, void *stream);
+/* Kernels per launch, work units, and the main kernel's time in the last launch
+ * (waits for it; pass NULL to skip). */
+LSGB_API int lsgb_plan_info(lsgb_plan *plan, uint32_t *kernels, uint64_t *units,
+                            float *last_kernel_ms);
+LSGB_API void lsgb_plan_destroy(lsgb_plan *plan);
+
 /* Tuning of the mixed kernel: frequencies per thread (F), threads per CTA, the
  * minimum CTAs per SM the kernel's register budget is compiled for, the packed
  * f32x2 inner loop (1) or the scalar one (0), and two observations per loop

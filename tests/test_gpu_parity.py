@@ -235,3 +235,54 @@ def test_plain_fp64_sincos_against_cuda(eng, scale):
     largest scale exercises the fallback to sincos() above 1e9 rad)."""
     err = eng.fp64_sincos_check(1 << 22, scale)
     assert err < 6e-16, err
+
+
+@pytest.mark.parametrize("variant,precision", [(0, "mixed"), (1, "mixed"), (0, "plain"), (1, "plain")])
+def test_plan_replays_direct_call_and_tracks_new_data(eng, variant, precision):
+    """A CUDA-graph plan gives the direct call's results, and follows data rewritten in
+    place between launches."""
+    import torch
+    dev = torch.device("cuda:0")
+    w = synth.lognormal_batch(seed=41 + variant, n_obj=40, n_freq=7000, error=bool(variant))
+    t = torch.from_numpy(w.t).to(dev)
+    y = torch.from_numpy(w.y).to(dev)
+    dy = torch.from_numpy(w.dy).to(dev) if variant else None
+
+    def outs():
+        return (torch.empty((w.n_obj, w.n_freq), dtype=torch.float64, device=dev),
+                torch.empty(w.n_obj, dtype=torch.int32, device=dev),
+                torch.empty(w.n_obj, dtype=torch.float64, device=dev))
+
+    pg_p, bi_p, bp_p = outs()
+    plan = eng.plan(variant, precision, t, y, dy, w.offsets, w.fmin, w.df, w.n_freq, variant == 0,
+                    pg_p, bi_p, bp_p)
+    for rep in range(2):
+        pg_d, bi_d, bp_d = outs()
+        eng.run_device(variant, precision, t, y, dy, w.offsets, w.fmin, w.df, w.n_freq,
+                       variant == 0, pg_d, bi_d, bp_d)
+        plan.launch()
+        torch.cuda.synchronize()
+        assert torch.equal(pg_p, pg_d) and torch.equal(bi_p, bi_d) and torch.equal(bp_p, bp_d)
+        y.mul_(-1.5).add_(0.25)  # new data of the same shape for the next launch
+    k, units, ms = plan.info(kernel_time=True)
+    assert k >= 3 and units > 0 and ms > 0
+    plan.close()
+
+
+def test_host_api_chunked_periodogram_copy(eng):
+    """A periodogram larger than one copy chunk (512 MiB) leaves in object chunks whose
+    copies overlap the next chunks' computation; the result equals the device path's."""
+    import torch
+    w = synth.lognormal_batch(seed=8, n_obj=300, n_freq=500_000)  # 300 x 5e5 x 8 B = 1.2 GB
+    r = eng.run_host(0, "mixed", w.t, w.y, None, w.offsets, w.fmin, w.df, w.n_freq,
+                     want_pgram=True)
+    dev = torch.device("cuda:0")
+    pg = torch.empty((w.n_obj, w.n_freq), dtype=torch.float64, device=dev)
+    bi = torch.empty(w.n_obj, dtype=torch.int32, device=dev)
+    bp = torch.empty(w.n_obj, dtype=torch.float64, device=dev)
+    eng.run_device(0, "mixed", torch.from_numpy(w.t).to(dev), torch.from_numpy(w.y).to(dev), None,
+                   w.offsets, w.fmin, w.df, w.n_freq, True, pg, bi, bp)
+    torch.cuda.synchronize()
+    assert np.array_equal(r.pgram, pg.cpu().numpy())
+    assert np.array_equal(r.best_idx, bi.cpu().numpy().astype(np.uint32))
+    assert np.array_equal(r.best_power, bp.cpu().numpy())
