@@ -1,8 +1,8 @@
 """Autotuner of the mixed kernel's shape, cached per (observation bucket, frequency bucket).
 
 The mixed kernel is compiled in several shapes (``engine.mixed_shapes()``): frequencies
-per thread F, threads per CTA, the register budget (minimum CTAs per SM), the packed
-f32x2 loop and the observation unroll. The fastest shape depends on the batch:
+per thread F, threads per CTA, the register budget (minimum CTAs per SM), the inner loop
+(scalar, packed f32x2 rotation, packed strided second-order) and the observation unroll. The fastest shape depends on the batch:
   * small objects amortize the per-(object, tile) staging and epilogue over few pairs;
   * few objects with few frequencies leave SMs idle unless tiles are small.
 The re-anchoring interval R is not tuned. In this design R equals F, because each

@@ -166,6 +166,9 @@ int plan_batch(Batch &b, int sms, const MixedShape *shapes, uint32_t reanchor, i
     const bool mixed = precision == LSGB_MIXED;
     b.shape = shapes[variant];
     b.reanchor = mixed ? reanchor : 0;
+    // the re-anchoring study is compiled for the consecutive-frequency packed loop only
+    if (b.reanchor) b.shape = variant == LSGB_STANDARD ? MixedShape{12, 256, 2, 1, 0}
+                                                       : MixedShape{8, 256, 2, 1, 0};
     const uint32_t tile_freqs = mixed ? (uint32_t)(b.shape.f * b.shape.nt) : (uint32_t)kPlainThreads;
     const uint64_t n_tiles64 = (n_freq + (uint64_t)tile_freqs - 1) / tile_freqs;
     b.units = n_tiles64 * n_obj;
@@ -176,10 +179,25 @@ int plan_batch(Batch &b, int sms, const MixedShape *shapes, uint32_t reanchor, i
     b.want_best = best_idx || best_power;
     int occ = 0;
     if (mixed) {
+        // Shared memory per CTA: at most what keeps the CTAs per SM that the shape's
+        // register budget allows resident (less the per-CTA reservation and the static
+        // variables), and at most kMixedSmemMax of staged records.
+        int dev = 0, smem_sm = 0;
+        LSGB_CUDA(cudaGetDevice(&dev));
+        LSGB_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+        const size_t per_cta = (size_t)smem_sm / (size_t)std::max(1, b.shape.minb) - 1024 - 256;
         const uint32_t rec_bytes = (uint32_t)mixed_rec_bytes(b.shape);
-        b.chunk = std::min<uint32_t>(max_n, kMixedSmemMax / rec_bytes);
+        size_t rec_budget = std::min<size_t>(kMixedSmemMax, per_cta);
+        b.chunk = (uint32_t)std::min<size_t>(max_n, rec_budget / rec_bytes);
         // objects longer than one chunk sum in two levels (chunk sums folded in smem)
         b.fold = max_n > b.chunk;
+        if (b.fold) {
+            const size_t fb = mixed_fold_bytes(variant, b.shape);
+            rec_budget = per_cta >= fb + 64 * (size_t)rec_bytes
+                             ? std::min<size_t>(kMixedSmemMax, per_cta - fb)
+                             : 64 * (size_t)rec_bytes;
+            b.chunk = (uint32_t)std::min<size_t>(max_n, rec_budget / rec_bytes);
+        }
         b.smem = (size_t)rec_bytes * b.chunk + (b.fold ? mixed_fold_bytes(variant, b.shape) : 0);
         LSGB_CUDA(mixed_occupancy(variant, dtype, b.shape, b.smem, &occ));
         if (occ < 1) return fail(LSGB_ERR_CUDA, "mixed kernel does not fit on an SM (smem %zu)", b.smem);
@@ -202,7 +220,7 @@ int upload_tables(const Batch &b, Workspace &ws, cudaStream_t st) {
     LSGB_CUDA(ws.counter.ensure(sizeof(uint32_t)));
     if (b.want_best && !mixed) LSGB_CUDA(ws.tile_best.ensure(sizeof(TileBest) * b.units));
     if (b.want_best && mixed) LSGB_CUDA(ws.keys.ensure(sizeof(unsigned long long) * b.n_obj));
-    if (mixed) LSGB_CUDA(ws.rec.ensure(sizeof(ObsRec) * b.rows));
+    if (mixed) LSGB_CUDA(ws.rec.ensure(mixed_global_rec_bytes(b.shape) * b.rows));
     LSGB_CUDA(cudaMemcpyAsync(ws.objs.p, b.objs.data(), sizeof(ObjInfo) * b.n_obj,
                               cudaMemcpyHostToDevice, st));
     LSGB_CUDA(cudaMemcpyAsync(ws.offs.p, b.offsets.data(), sizeof(uint64_t) * (b.n_obj + 1),
@@ -237,10 +255,11 @@ int enqueue_batch(Batch &b, Workspace &ws, cudaStream_t st, cudaEvent_t ev0, cud
         two_prod(b.fmin, kInv2PiHi, kInv2PiLo, g.f0_hi, g.f0_lo);
         two_prod(b.df, kInv2PiHi, kInv2PiLo, g.df_hi, g.df_lo);
         LSGB_CUDA(launch_records(b.variant, b.dtype, b.t, b.y, b.dy, (const uint64_t *)ws.offs.p,
-                                 b.n_obj, d_objs, b.rows, g, (ObsRec *)ws.rec.p, st));
+                                 b.n_obj, d_objs, b.rows, g, ws.rec.p,
+                                 b.shape.x2 == 2 ? (uint32_t)b.shape.nt : 0u, st));
         ++kernels;
         MixedArgs a{};
-        a.rec = (const ObsRec *)ws.rec.p;
+        a.rec = ws.rec.p;
         a.objs = d_objs;
         a.perm = (const uint32_t *)ws.perm.p;
         a.n_obj = b.n_obj;
@@ -305,7 +324,9 @@ struct lsgb_engine {
     cudaStream_t d2h = nullptr;     // host-buffer API: periodogram copies overlapping compute
     Workspace ws;
     DevBuf in_t, in_y, in_dy, out_pg, out_idx, out_p;
-    MixedShape shape[2] = {{12, 256, 2, 1, 0}, {8, 256, 2, 1, 0}};
+    // defaults measured fastest on the 999-object, 1e6-frequency batches: the strided
+    // second-order loop for both variants
+    MixedShape shape[2] = {{12, 256, 2, 2, 0}, {10, 256, 2, 2, 0}};
     uint32_t last_kernels = 0;
     uint64_t last_units = 0;
     cudaEvent_t ev_main0 = nullptr, ev_main1 = nullptr;  // around the last main-kernel launch
@@ -379,7 +400,7 @@ LSGB_API int lsgb_set_tuning(lsgb_engine *eng, int variant, int f, int nt, int m
     if (f > 0) s.f = f;
     if (nt > 0) s.nt = nt;
     if (minb > 0) s.minb = minb;
-    if (x2 >= 0) s.x2 = x2 ? 1 : 0;
+    if (x2 >= 0) s.x2 = x2 > 2 ? -1 : x2;  // -1 matches no compiled shape
     if (unroll >= 0) s.uj = unroll ? 1 : 0;
     int blocks = 0;
     if (mixed_occupancy(variant, LSGB_F32, s, 1024, &blocks) != cudaSuccess)
@@ -610,7 +631,8 @@ LSGB_API int lsgb_periodogram_host(lsgb_engine *eng, int variant, int precision,
             LSGB_CUDA(eng->ws.perm.ensure(sizeof(uint32_t) * n_obj));
             LSGB_CUDA(eng->ws.counter.ensure(sizeof(uint32_t)));
             LSGB_CUDA(eng->ws.keys.ensure(sizeof(unsigned long long) * n_obj));
-            if (precision == LSGB_MIXED) LSGB_CUDA(eng->ws.rec.ensure(sizeof(ObsRec) * rows));
+            if (precision == LSGB_MIXED)
+                LSGB_CUDA(eng->ws.rec.ensure(mixed_global_rec_bytes(eng->shape[variant]) * rows));
             else if (best_idx || best_power)
                 LSGB_CUDA(eng->ws.tile_best.ensure(sizeof(TileBest) * max_tiles * n_obj));
         }

@@ -20,6 +20,30 @@ struct __align__(16) ObsRec {
 };
 static_assert(sizeof(ObsRec) == 32, "ObsRec must be 32 bytes");
 
+// One observation for the second-order form of the packed loop (96 bytes, six 16-byte
+// quads laid out as the kernel reads them from shared memory; each 64-bit half of q1..q5
+// is a ready-made f32x2 operand). A thread of that form takes the frequencies
+// k0, k0 + S, k0 + 2S, ... (S = threads per CTA) as pairs (k0 + 2mS, k0 + (2m+1)S); both
+// lanes of a pair advance by the angle phi = 2 S (2 pi b) per step, with
+//   x[m+1] = 2 cos(phi) x[m] - x[m-1]
+// when |sin phi| >= kSecondOrderMinSin (two operations per lane instead of the four of a
+// rotation), else by the rotation. With u = S (2 pi b):
+//   q0 = {a_lo, a_hi, b_lo, b_hi}            (as ObsRec)
+//   q1 = {v0, v0, cos u, sin u}              (the odd lane's offset from the anchor)
+//   q2 = {cos phi, cos phi, sin phi, sin phi}
+//   q3 = {-sin phi, -sin phi, v1, v1}
+//   q4 = {K, K, -K, -K},  K = 2 cos phi      (rounded once from FP64)
+//   q5 = {-cos phi, -cos phi, well, 0}       (well = 1: |sin phi| >= kSecondOrderMinSin)
+// All trigonometric values are computed in FP64 from the exact fixed-point phase S*b.
+struct __align__(16) SoRec {
+    uint4 q[6];
+};
+static_assert(sizeof(SoRec) == 96, "SoRec must be 96 bytes");
+// Below this |sin phi| the rounding of K = 2 cos phi (up to 2^-24) would move the
+// recurrence's angle by more than 2^-24 / (2 |sin phi|) per step, so such observations
+// take the rotation.
+constexpr double kSecondOrderMinSin = 0.125;
+
 // Per-object parameters, indexed by the caller's object index.
 struct ObjInfo {
     uint64_t row0;  // first row of the object in t / y / dy / records
@@ -51,7 +75,7 @@ struct GridTurns {
 };
 
 struct MixedArgs {
-    const ObsRec *rec;
+    const void *rec;       // ObsRec or SoRec records (per the shape)
     const ObjInfo *objs;
     const uint32_t *perm;  // work order: objects by decreasing size
     uint32_t n_obj, n_tiles, n_freq, chunk;
@@ -82,11 +106,15 @@ struct PlainArgs {
 // and the minimum CTAs per SM its register budget is compiled for.
 struct MixedShape {
     int f, nt, minb;
-    int x2;  // 1: packed f32x2 loop (two interleaved frequency chains per thread)
+    int x2;  // 0: scalar loop; 1: packed f32x2 loop (two interleaved frequency chains per
+             // thread, rotation steps); 2: packed loop with strided frequencies and
+             // second-order recurrence steps (SoRec records)
     int uj;  // 1: two observations per inner-loop iteration (independent chains), 0: one
 };
 // Bytes of shared memory per staged observation of a mixed shape.
-inline int mixed_rec_bytes(const MixedShape &s) { return s.x2 ? 64 : 32; }
+inline int mixed_rec_bytes(const MixedShape &s) { return s.x2 == 2 ? 96 : (s.x2 ? 64 : 32); }
+// Bytes of the device record of one observation (ObsRec or SoRec).
+inline size_t mixed_global_rec_bytes(const MixedShape &s) { return s.x2 == 2 ? 96 : 32; }
 // Bytes of the second-level sum area of a mixed shape (NA sums x F x threads floats).
 inline size_t mixed_fold_bytes(int variant, const MixedShape &s) {
     return (size_t)(variant ? 6 : 4) * s.f * s.nt * sizeof(float);
@@ -95,14 +123,17 @@ inline size_t mixed_fold_bytes(int variant, const MixedShape &s) {
 // ---- launchers (lsgb_kernels.cu); all asynchronous on `st` ----
 cudaError_t launch_stats(int variant, int mixed, int dtype, int normalize, const void *y,
                          const void *dy, ObjInfo *objs, uint32_t n_obj, cudaStream_t st);
+// so_stride 0: ObsRec records; > 0: SoRec records for a second-order shape whose CTA
+// has so_stride threads. `rec` holds rows x 32 or rows x 96 bytes accordingly.
 cudaError_t launch_records(int variant, int dtype, const void *t, const void *y, const void *dy,
                            const uint64_t *offsets, uint32_t n_obj, const ObjInfo *objs,
-                           uint64_t rows, GridTurns g, ObsRec *rec, cudaStream_t st);
+                           uint64_t rows, GridTurns g, void *rec, uint32_t so_stride,
+                           cudaStream_t st);
 // Mixed kernel: returns cudaErrorInvalidValue when (variant, dtype, shape) is not compiled.
 cudaError_t launch_mixed(int variant, int dtype, MixedShape shape, const MixedArgs &a,
                          int grid, size_t smem, cudaStream_t st);
 cudaError_t mixed_occupancy(int variant, int dtype, MixedShape shape, size_t smem, int *blocks);
-// Compiled mixed shapes as (variant, F, threads, min CTAs, packed) quintuples; returns the count.
+// Compiled mixed shapes as (variant, F, threads, min CTAs, packed, unroll); returns the count.
 int mixed_shapes(int *out, int max_shapes);
 cudaError_t launch_plain(int variant, int in_dtype, int out_dtype, const PlainArgs &a, int grid,
                          size_t smem, cudaStream_t st);

@@ -183,14 +183,18 @@ __global__ void stats_kernel(int variant, int mixed, int dtype, int normalize, c
 // ---------------------------------------------------------------------------
 __global__ void records_kernel(int variant, int dtype, const void *t, const void *y,
                                const void *dy, const uint64_t *offsets, uint32_t n_obj,
-                               const ObjInfo *objs, uint64_t rows, GridTurns g, ObsRec *rec) {
+                               const ObjInfo *objs, uint64_t rows, GridTurns g, void *rec,
+                               uint32_t so_stride) {
     for (uint64_t row = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; row < rows;
          row += (uint64_t)gridDim.x * blockDim.x) {
         const double td = load_in(dtype, t, row);
         const uint64_t a = frac_turns_u64(g.f0_hi, g.f0_lo, td);
         const uint64_t b = frac_turns_u64(g.df_hi, g.df_lo, td);
+        // the step of the recurrence: one grid point, or so_stride of them (exact in the
+        // fixed-point turns; the signed reading puts the angle in [-pi, pi))
+        const uint64_t bs = so_stride ? b * (uint64_t)so_stride : b;
         double sd, cd;
-        sincos((double)(long long)b * kTwoPiOver2p64, &sd, &cd);
+        sincos((double)(long long)bs * kTwoPiOver2p64, &sd, &cd);
         ObsRec r;
         r.a_lo = (uint32_t)a;
         r.a_hi = (uint32_t)(a >> 32);
@@ -215,8 +219,24 @@ __global__ void records_kernel(int variant, int dtype, const void *t, const void
             r.v0 = (float)wn;
             r.v1 = (float)(wn * (load_in(dtype, y, row) - ob.ymean));
         }
-        reinterpret_cast<uint4 *>(rec + row)[0] = make_uint4(r.a_lo, r.a_hi, r.b_lo, r.b_hi);
-        reinterpret_cast<float4 *>(rec + row)[1] = make_float4(r.v0, r.v1, r.cd, r.sd);
+        if (!so_stride) {
+            uint4 *d = reinterpret_cast<uint4 *>(static_cast<ObsRec *>(rec) + row);
+            d[0] = make_uint4(r.a_lo, r.a_hi, r.b_lo, r.b_hi);
+            reinterpret_cast<float4 *>(d)[1] = make_float4(r.v0, r.v1, r.cd, r.sd);
+        } else {
+            // the pair step phi = 2 so_stride grid points
+            double s2, c2;
+            sincos((double)(long long)(bs * 2u) * kTwoPiOver2p64, &s2, &c2);
+            const float fc2 = (float)c2, fs2 = (float)s2, K = (float)(2.0 * c2);
+            const uint32_t well = fabs(s2) >= kSecondOrderMinSin ? 1u : 0u;
+            uint4 *d = static_cast<SoRec *>(rec)[row].q;
+            d[0] = make_uint4(r.a_lo, r.a_hi, r.b_lo, r.b_hi);
+            reinterpret_cast<float4 *>(d)[1] = make_float4(r.v0, r.v0, r.cd, r.sd);
+            reinterpret_cast<float4 *>(d)[2] = make_float4(fc2, fc2, fs2, fs2);
+            reinterpret_cast<float4 *>(d)[3] = make_float4(-fs2, -fs2, r.v1, r.v1);
+            reinterpret_cast<float4 *>(d)[4] = make_float4(K, K, -K, -K);
+            d[5] = make_uint4(__float_as_uint(-fc2), __float_as_uint(-fc2), well, 0u);
+        }
     }
 }
 
@@ -308,20 +328,60 @@ __device__ __forceinline__ void unpack2(uint64_t v, float &lo, float &hi) {
 //   q1 = {v0, v0, cd, sd}            ({y,y} or {w,w}; the single step for the odd chain)
 //   q2 = {cd2, cd2, sd2, sd2}        (the double step of both chains)
 //   q3 = {-sd2, -sd2, v1, v1}        ({wy, wy} for the generalized variant)
-// Each 64-bit half of q1..q3 is a ready-made packed operand.
+// Each 64-bit half of q1..q3 is a ready-made packed operand. The second-order form
+// (PK = 2) stages SoRec records (lsgb_internal.h) as they are.
 constexpr int kX2RecBytes = 64;
 
-template <int F, int NT, int MINB, bool GEN, bool X2, int UJ, bool RA, typename OutT>
+// Accumulates one packed pair of frequencies: (cos, sin) pairs C, S with the weights V0
+// (y, or w) and V1 (w y', generalized).
+template <bool GEN, int NA, int NP>
+__device__ __forceinline__ void accumulate_pair(uint64_t (&acc2)[NA][NP], int pp, uint64_t V0,
+                                                uint64_t V1, uint64_t C, uint64_t S) {
+    if (!GEN) {
+        acc2[0][pp] = ffma2(V0, C, acc2[0][pp]);  // XC
+        acc2[1][pp] = ffma2(V0, S, acc2[1][pp]);  // XS
+        acc2[2][pp] = ffma2(C, C, acc2[2][pp]);   // CC
+        acc2[3][pp] = ffma2(C, S, acc2[3][pp]);   // CS
+    } else {
+        const uint64_t WC = fmul2(V0, C);
+        acc2[0][pp] = fadd2(acc2[0][pp], WC);     // C
+        acc2[1][pp] = ffma2(V0, S, acc2[1][pp]);  // S
+        acc2[2][pp] = ffma2(V1, C, acc2[2][pp]);  // YC
+        acc2[3][pp] = ffma2(V1, S, acc2[3][pp]);  // YS
+        acc2[4][pp] = ffma2(WC, C, acc2[4][pp]);  // CC
+        acc2[5][pp] = ffma2(WC, S, acc2[5][pp]);  // CS
+    }
+}
+
+// Mixed kernel, PK selects the inner loop:
+//   0  scalar: F consecutive frequencies per thread, rotation steps;
+//   1  packed f32x2: the same run as two interleaved chains (even / odd frequencies),
+//      pair p = (k0 + 2p, k0 + 2p + 1), rotation steps of two grid points;
+//   2  packed f32x2, strided: frequencies k0 + i NT (i < F), pair p = (k0 + 2p NT,
+//      k0 + (2p+1) NT), steps of phi = 2 NT grid points by the second-order recurrence
+//      x[p+1] = K x[p] - x[p-1], K = 2 cos phi, where it is well conditioned (SoRec).
+// In form 2 the recurrence runs on sign-flipped values y[p] = sigma[p] x[p] with
+// sigma = (+, +, -, -, +, +, ...), for which y[p+1] = (+-K) y[p] + y[p-1] needs no
+// negation; the sums linear in (cos, sin) take the sign, the quadratic ones do not, and
+// the epilogue flips it back. The rotation path of ill-conditioned observations produces
+// the same signed values (by negated rotations where sigma changes).
+template <int F, int NT, int MINB, bool GEN, int PK, int UJ, bool RA, typename OutT>
 __global__ void __launch_bounds__(NT, MINB) mixed_kernel(MixedArgs a) {
+    constexpr bool X2 = PK != 0;
+    constexpr bool SO = PK == 2;
+    static_assert(!(SO && RA), "re-anchoring applies to the consecutive-frequency forms");
+    constexpr int RQ = SO ? 6 : (X2 ? 4 : 2);  // 16-byte quads per staged observation
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    uint4 *s_rec = reinterpret_cast<uint4 *>(smem_raw);  // 2 x uint4 per observation
+    uint4 *s_rec = reinterpret_cast<uint4 *>(smem_raw);  // RQ x uint4 per observation
     // second-level sums of objects longer than one staged chunk, private per thread:
     // s_fold[(q * F + f) * NT + tid]; present when a.fold != 0
-    float *s_fold = reinterpret_cast<float *>(smem_raw + (size_t)a.chunk * (X2 ? kX2RecBytes : 32));
+    float *s_fold = reinterpret_cast<float *>(smem_raw + (size_t)a.chunk * (16 * RQ));
     __shared__ uint32_t s_unit;
     __shared__ float s_bp[NT / 32];
     __shared__ uint32_t s_bk[NT / 32];
     constexpr int NA = GEN ? 6 : 4;
+    // frequency f of a thread is k0 + f * KS
+    constexpr uint32_t KS = SO ? NT : 1;
     const uint32_t units = a.n_obj * a.n_tiles;
 
     for (;;) {
@@ -333,10 +393,8 @@ __global__ void __launch_bounds__(NT, MINB) mixed_kernel(MixedArgs a) {
         const uint32_t tile = u - (u / a.n_tiles) * a.n_tiles;
         const uint64_t row0 = a.objs[o].row0;
         const uint32_t n = a.objs[o].n;
-        const uint32_t k0 = tile * (uint32_t)(NT * F) + threadIdx.x * (uint32_t)F;
+        const uint32_t k0 = tile * (uint32_t)(NT * F) + threadIdx.x * (uint32_t)(SO ? 1 : F);
 
-        // X2: two interleaved chains (even / odd frequencies of the run) advance by 2 steps
-        // as packed pairs; accumulator pair p holds frequencies (k0+2p, k0+2p+1).
         static_assert(!X2 || F % 2 == 0, "the packed loop needs an even F");
         constexpr int NP = X2 ? F / 2 : 1;
         float acc[NA][F];
@@ -356,10 +414,16 @@ __global__ void __launch_bounds__(NT, MINB) mixed_kernel(MixedArgs a) {
         }
         for (uint32_t c0 = 0; c0 < n; c0 += a.chunk) {
             const uint32_t cnt = min(a.chunk, n - c0);
-            const uint4 *src = reinterpret_cast<const uint4 *>(a.rec + row0 + c0);
-            if (!X2) {
+            if (SO) {
+                const uint4 *src = reinterpret_cast<const SoRec *>(a.rec)[row0 + c0].q;
+                for (uint32_t i = threadIdx.x; i < 6 * cnt; i += NT) s_rec[i] = __ldg(src + i);
+            } else if (!X2) {
+                const uint4 *src = reinterpret_cast<const uint4 *>(
+                    static_cast<const ObsRec *>(a.rec) + row0 + c0);
                 for (uint32_t i = threadIdx.x; i < 2 * cnt; i += NT) s_rec[i] = __ldg(src + i);
             } else {
+                const uint4 *src = reinterpret_cast<const uint4 *>(
+                    static_cast<const ObsRec *>(a.rec) + row0 + c0);
                 for (uint32_t i = threadIdx.x; i < cnt; i += NT) {
                     const uint4 q0 = __ldg(src + 2 * i);
                     const uint4 qv = __ldg(src + 2 * i + 1);
@@ -374,20 +438,34 @@ __global__ void __launch_bounds__(NT, MINB) mixed_kernel(MixedArgs a) {
                 }
             }
             __syncthreads();
-#pragma unroll UJ
-            for (uint32_t j = 0; j < cnt; ++j) {
-                const uint4 ab = X2 ? s_rec[4 * j] : s_rec[2 * j];
-                // anchor: top 32 bits of a + ka*b (mod 2^64), as a signed turn count; ka is
-                // the thread's first frequency, or with re-anchoring every R grid points
-                // the R-aligned point below it
-                const uint32_t adv = RA ? k0 % a.reanchor : 0u;
-                const uint32_t ka = k0 - adv;
+            // anchor: top 32 bits of a + ka*b (mod 2^64), as a signed turn count; ka is
+            // the thread's first frequency, or with re-anchoring every R grid points the
+            // R-aligned point below it. In the scalar loop the anchor of observation j+1 is
+            // computed during observation j, off the critical path of its recurrence (the
+            // packed loops measured faster without this).
+            constexpr bool PIPE = !X2;
+            const uint32_t adv = RA ? k0 % a.reanchor : 0u;
+            const uint32_t ka = k0 - adv;
+            auto anchor = [&](uint32_t jj, float &sa, float &ca) {
+                const uint4 ab = s_rec[RQ * jj];
                 const uint64_t p = (uint64_t)ka * ab.z + (((uint64_t)ab.y << 32) | ab.x);
                 const uint32_t hi = (uint32_t)(p >> 32) + ka * ab.w;
+                __sincosf((float)(int32_t)hi * kTwoPiOver2p32f, &sa, &ca);
+            };
+            float s_next = 0.0f, c_next = 0.0f;
+            if (PIPE) anchor(0, s_next, c_next);
+#pragma unroll UJ
+            for (uint32_t j = 0; j < cnt; ++j) {
                 float s, c;
-                __sincosf((float)(int32_t)hi * kTwoPiOver2p32f, &s, &c);
+                if (PIPE) {
+                    s = s_next;
+                    c = c_next;
+                    anchor(min(j + 1, cnt - 1), s_next, c_next);
+                } else {
+                    anchor(j, s, c);
+                }
                 if (RA && adv) {
-                    const float4 v = reinterpret_cast<const float4 *>(s_rec)[X2 ? 4 * j + 1 : 2 * j + 1];
+                    const float4 v = reinterpret_cast<const float4 *>(s_rec)[RQ * j + 1];
                     const float cd = v.z, sd = v.w;  // same place in both layouts
                     for (uint32_t q = 0; q < adv; ++q) {
                         const float cn = fmaf(c, cd, -s * sd);
@@ -420,36 +498,70 @@ __global__ void __launch_bounds__(NT, MINB) mixed_kernel(MixedArgs a) {
                         }
                     }
                 } else {
-                    const ulonglong2 q1 = reinterpret_cast<const ulonglong2 *>(s_rec)[4 * j + 1];
-                    const ulonglong2 q2 = reinterpret_cast<const ulonglong2 *>(s_rec)[4 * j + 2];
-                    const ulonglong2 q3 = reinterpret_cast<const ulonglong2 *>(s_rec)[4 * j + 3];
+                    const ulonglong2 *R = reinterpret_cast<const ulonglong2 *>(s_rec) + RQ * j;
+                    const ulonglong2 q1 = R[1], q2 = R[2], q3 = R[3];
                     float cd, sd;
                     unpack2(q1.y, cd, sd);
-                    const float c1 = fmaf(c, cd, -s * sd);  // odd chain: one step ahead
+                    const float c1 = fmaf(c, cd, -s * sd);  // odd lane: one step (or NT) ahead
                     const float s1 = fmaf(s, cd, c * sd);
                     uint64_t C = pack2(c, c1), S = pack2(s, s1);
                     const uint64_t V0 = q1.x, CD2 = q2.x, SD2 = q2.y, NSD2 = q3.x, V1 = q3.y;
+                    if (!SO) {
 #pragma unroll
-                    for (int pp = 0; pp < NP; ++pp) {
-                        if (!GEN) {
-                            acc2[0][pp] = ffma2(V0, C, acc2[0][pp]);  // XC
-                            acc2[1][pp] = ffma2(V0, S, acc2[1][pp]);  // XS
-                            acc2[2][pp] = ffma2(C, C, acc2[2][pp]);   // CC
-                            acc2[3][pp] = ffma2(C, S, acc2[3][pp]);   // CS
-                        } else {
-                            const uint64_t WC = fmul2(V0, C);
-                            acc2[0][pp] = fadd2(acc2[0][pp], WC);     // C
-                            acc2[1][pp] = ffma2(V0, S, acc2[1][pp]);  // S
-                            acc2[2][pp] = ffma2(V1, C, acc2[2][pp]);  // YC
-                            acc2[3][pp] = ffma2(V1, S, acc2[3][pp]);  // YS
-                            acc2[4][pp] = ffma2(WC, C, acc2[4][pp]);  // CC
-                            acc2[5][pp] = ffma2(WC, S, acc2[5][pp]);  // CS
+                        for (int pp = 0; pp < NP; ++pp) {
+                            accumulate_pair<GEN>(acc2, pp, V0, V1, C, S);
+                            if (pp + 1 < NP) {
+                                const uint64_t t1 = fmul2(S, NSD2);
+                                const uint64_t t2 = fmul2(C, SD2);
+                                C = ffma2(C, CD2, t1);
+                                S = ffma2(S, CD2, t2);
+                            }
                         }
-                        if (pp + 1 < NP) {
+                    } else {
+                        accumulate_pair<GEN>(acc2, 0, V0, V1, C, S);
+                        // pair 1 by a rotation (sigma[1] = sigma[0])
+                        uint64_t Cp = C, Sp = S;
+                        if (NP > 1) {
                             const uint64_t t1 = fmul2(S, NSD2);
                             const uint64_t t2 = fmul2(C, SD2);
                             C = ffma2(C, CD2, t1);
                             S = ffma2(S, CD2, t2);
+                            accumulate_pair<GEN>(acc2, 1, V0, V1, C, S);
+                        }
+                        const ulonglong2 q5 = R[5];
+                        if ((uint32_t)q5.y) {
+                            // well conditioned: y[p] = A[p] y[p-1] + y[p-2], A[p] = -K for
+                            // even p, +K for odd p
+                            const ulonglong2 q4 = R[4];
+#pragma unroll
+                            for (int pp = 2; pp < NP; ++pp) {
+                                const uint64_t A = (pp & 1) ? q4.x : q4.y;
+                                const uint64_t Cn = ffma2(A, C, Cp);
+                                const uint64_t Sn = ffma2(A, S, Sp);
+                                Cp = C;
+                                Sp = S;
+                                C = Cn;
+                                S = Sn;
+                                accumulate_pair<GEN>(acc2, pp, V0, V1, C, S);
+                            }
+                        } else {
+                            // rotation; negated where sigma changes sign (even p)
+                            const uint64_t NCD2 = q5.x;
+#pragma unroll
+                            for (int pp = 2; pp < NP; ++pp) {
+                                if (pp & 1) {
+                                    const uint64_t t1 = fmul2(S, NSD2);
+                                    const uint64_t t2 = fmul2(C, SD2);
+                                    C = ffma2(C, CD2, t1);
+                                    S = ffma2(S, CD2, t2);
+                                } else {
+                                    const uint64_t t1 = fmul2(S, SD2);
+                                    const uint64_t t2 = fmul2(C, NSD2);
+                                    C = ffma2(C, NCD2, t1);
+                                    S = ffma2(S, NCD2, t2);
+                                }
+                                accumulate_pair<GEN>(acc2, pp, V0, V1, C, S);
+                            }
                         }
                     }
                 }
@@ -492,6 +604,14 @@ __global__ void __launch_bounds__(NT, MINB) mixed_kernel(MixedArgs a) {
                     unpack2(acc2[q][pp], acc[q][2 * pp], acc[q][2 * pp + 1]);
                 }
         }
+        if (SO) {
+            // undo sigma on the sums linear in (cos, sin): pairs 2, 3 (mod 4)
+#pragma unroll
+            for (int q = 0; q < (GEN ? 4 : 2); ++q)
+#pragma unroll
+                for (int f = 0; f < F; ++f)
+                    if ((f >> 2) & 1) acc[q][f] = -acc[q][f];
+        }
 
         // epilogue: power, optional store, thread-local first maximum (all FP32: the
         // FP64 pipe of this part is 1/64 of the FP32 rate)
@@ -504,7 +624,7 @@ __global__ void __launch_bounds__(NT, MINB) mixed_kernel(MixedArgs a) {
             const float N = (float)n;
 #pragma unroll
             for (int f = 0; f < F; ++f) {
-                const uint32_t k = k0 + f;
+                const uint32_t k = k0 + f * KS;
                 const float P = std_power_f(N, acc[0][f], acc[1][f], acc[2][f], acc[3][f]) * nrm;
                 if (k < a.n_freq) {
                     if (a.pgram) store_out<OutT>(a.pgram, out0 + k, P);
@@ -516,7 +636,7 @@ __global__ void __launch_bounds__(NT, MINB) mixed_kernel(MixedArgs a) {
             const float ybar = a.objs[o].ybar32;
 #pragma unroll
             for (int f = 0; f < F; ++f) {
-                const uint32_t k = k0 + f;
+                const uint32_t k = k0 + f * KS;
                 const float P = gen_power_f(invW, ybar, acc[0][f], acc[1][f], acc[2][f], acc[3][f],
                                             acc[4][f], acc[5][f]) * nrm;
                 if (k < a.n_freq) {
@@ -827,15 +947,15 @@ __global__ void key_decode_kernel(const unsigned long long *keys, uint32_t n_obj
     if (best_power) best_power[o] = (OutT)__uint_as_float((uint32_t)(k >> 32));
 }
 
-template <int F, int NT, int MINB, bool GEN, bool X2, int UJ, bool RA>
+template <int F, int NT, int MINB, bool GEN, int PK, int UJ, bool RA>
 cudaError_t launch_mixed_t(int dtype, const MixedArgs &a, int grid, size_t smem, cudaStream_t st) {
     if (dtype == 0) {
-        auto k = mixed_kernel<F, NT, MINB, GEN, X2, UJ, RA, float>;
+        auto k = mixed_kernel<F, NT, MINB, GEN, PK, UJ, RA, float>;
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         k<<<grid, NT, smem, st>>>(a);
     } else {
-        auto k = mixed_kernel<F, NT, MINB, GEN, X2, UJ, RA, double>;
+        auto k = mixed_kernel<F, NT, MINB, GEN, PK, UJ, RA, double>;
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         k<<<grid, NT, smem, st>>>(a);
@@ -843,15 +963,15 @@ cudaError_t launch_mixed_t(int dtype, const MixedArgs &a, int grid, size_t smem,
     return cudaGetLastError();
 }
 
-template <int F, int NT, int MINB, bool GEN, bool X2, int UJ, bool RA>
+template <int F, int NT, int MINB, bool GEN, int PK, int UJ, bool RA>
 cudaError_t occ_mixed_t(int dtype, size_t smem, int *blocks) {
     cudaError_t e;
     if (dtype == 0) {
-        auto k = mixed_kernel<F, NT, MINB, GEN, X2, UJ, RA, float>;
+        auto k = mixed_kernel<F, NT, MINB, GEN, PK, UJ, RA, float>;
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k, NT, smem);
     } else {
-        auto k = mixed_kernel<F, NT, MINB, GEN, X2, UJ, RA, double>;
+        auto k = mixed_kernel<F, NT, MINB, GEN, PK, UJ, RA, double>;
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k, NT, smem);
     }
@@ -859,22 +979,29 @@ cudaError_t occ_mixed_t(int dtype, size_t smem, int *blocks) {
 }
 
 // The compiled mixed shapes: (frequencies per thread, threads, min CTAs per SM for
-// the register budget, generalized?, packed f32x2 loop?, observations per iteration,
-// re-anchoring study variant?). Study variants are chosen by lsgb_set_reanchor, not
-// listed as tuning shapes.
-#define LSGB_MIXED_SHAPES(X)                \
-    X(16, 256, 2, false, false, 1, false)   \
-    X(8, 256, 3, false, false, 1, false)    \
-    X(12, 256, 2, false, true, 1, false)    \
-    X(12, 128, 4, false, true, 1, false)    \
-    X(10, 256, 2, false, true, 1, false)    \
-    X(8, 256, 3, false, true, 1, false)     \
-    X(12, 256, 2, true, false, 1, false)    \
-    X(8, 256, 2, true, true, 1, false)      \
-    X(8, 128, 4, true, true, 1, false)      \
-    X(10, 256, 2, true, true, 1, false)     \
-    X(12, 256, 2, false, true, 1, true)     \
-    X(8, 256, 2, true, true, 1, true)
+// the register budget, generalized?, inner loop form (0 scalar, 1 packed rotation,
+// 2 packed second-order), observations per iteration, re-anchoring study variant?).
+// Study variants are chosen by lsgb_set_reanchor, not listed as tuning shapes.
+#define LSGB_MIXED_SHAPES(X)            \
+    X(16, 256, 2, false, 0, 1, false)   \
+    X(8, 256, 3, false, 0, 1, false)    \
+    X(12, 256, 2, false, 1, 1, false)   \
+    X(12, 128, 4, false, 1, 1, false)   \
+    X(10, 256, 2, false, 1, 1, false)   \
+    X(8, 256, 3, false, 1, 1, false)    \
+    X(12, 256, 2, false, 2, 1, false)   \
+    X(16, 256, 2, false, 2, 1, false)   \
+    X(8, 256, 3, false, 2, 1, false)    \
+    X(10, 256, 3, false, 2, 1, false)   \
+    X(12, 256, 2, true, 0, 1, false)    \
+    X(8, 256, 2, true, 1, 1, false)     \
+    X(8, 128, 4, true, 1, 1, false)     \
+    X(10, 256, 2, true, 1, 1, false)    \
+    X(8, 256, 2, true, 2, 1, false)     \
+    X(6, 256, 3, true, 2, 1, false)     \
+    X(10, 256, 2, true, 2, 1, false)    \
+    X(12, 256, 2, false, 1, 1, true)    \
+    X(8, 256, 2, true, 1, 1, true)
 
 }  // namespace
 
@@ -887,21 +1014,22 @@ cudaError_t launch_stats(int variant, int mixed, int dtype, int normalize, const
 
 cudaError_t launch_records(int variant, int dtype, const void *t, const void *y, const void *dy,
                            const uint64_t *offsets, uint32_t n_obj, const ObjInfo *objs,
-                           uint64_t rows, GridTurns g, ObsRec *rec, cudaStream_t st) {
+                           uint64_t rows, GridTurns g, void *rec, uint32_t so_stride,
+                           cudaStream_t st) {
     if (rows == 0) return cudaSuccess;
     const uint64_t blocks64 = (rows + 255) / 256;
     const int blocks = (int)(blocks64 < 65535ull * 16 ? blocks64 : 65535ull * 16);
     records_kernel<<<blocks, 256, 0, st>>>(variant, dtype, t, y, dy, offsets, n_obj, objs, rows, g,
-                                           rec);
+                                           rec, so_stride);
     return cudaGetLastError();
 }
 
 cudaError_t launch_mixed(int variant, int dtype, MixedShape shape, const MixedArgs &a, int grid,
                          size_t smem, cudaStream_t st) {
-#define X(F_, NT_, MB_, G_, X2_, UJ_, RA_)                                           \
+#define X(F_, NT_, MB_, G_, PK_, UJ_, RA_)                                           \
     if (shape.f == F_ && shape.nt == NT_ && shape.minb == MB_ && (variant == 1) == G_ && \
-        (shape.x2 != 0) == X2_ && (shape.uj ? 2 : 1) == UJ_ && (a.reanchor != 0) == RA_) \
-        return launch_mixed_t<F_, NT_, MB_, G_, X2_, UJ_, RA_>(dtype, a, grid, smem, st);
+        shape.x2 == PK_ && (shape.uj ? 2 : 1) == UJ_ && (a.reanchor != 0) == RA_)        \
+        return launch_mixed_t<F_, NT_, MB_, G_, PK_, UJ_, RA_>(dtype, a, grid, smem, st);
     LSGB_MIXED_SHAPES(X)
 #undef X
     return cudaErrorInvalidValue;
@@ -909,14 +1037,14 @@ cudaError_t launch_mixed(int variant, int dtype, MixedShape shape, const MixedAr
 
 int mixed_shapes(int *out, int max_shapes) {
     int n = 0;
-#define X(F_, NT_, MB_, G_, X2_, UJ_, RA_)       \
+#define X(F_, NT_, MB_, G_, PK_, UJ_, RA_)       \
     if (RA_) {                                   \
     } else if (out && n < max_shapes) {          \
         out[6 * n + 0] = G_ ? 1 : 0;             \
         out[6 * n + 1] = F_;                     \
         out[6 * n + 2] = NT_;                    \
         out[6 * n + 3] = MB_;                    \
-        out[6 * n + 4] = X2_ ? 1 : 0;            \
+        out[6 * n + 4] = PK_;                    \
         out[6 * n + 5] = UJ_ == 2 ? 1 : 0;       \
     }                                            \
     n += RA_ ? 0 : 1;
@@ -926,10 +1054,10 @@ int mixed_shapes(int *out, int max_shapes) {
 }
 
 cudaError_t mixed_occupancy(int variant, int dtype, MixedShape shape, size_t smem, int *blocks) {
-#define X(F_, NT_, MB_, G_, X2_, UJ_, RA_)                                           \
+#define X(F_, NT_, MB_, G_, PK_, UJ_, RA_)                                           \
     if (shape.f == F_ && shape.nt == NT_ && shape.minb == MB_ && (variant == 1) == G_ && \
-        (shape.x2 != 0) == X2_ && (shape.uj ? 2 : 1) == UJ_ && !RA_)                     \
-        return occ_mixed_t<F_, NT_, MB_, G_, X2_, UJ_, RA_>(dtype, smem, blocks);
+        shape.x2 == PK_ && (shape.uj ? 2 : 1) == UJ_ && !RA_)                            \
+        return occ_mixed_t<F_, NT_, MB_, G_, PK_, UJ_, RA_>(dtype, smem, blocks);
     LSGB_MIXED_SHAPES(X)
 #undef X
     return cudaErrorInvalidValue;

@@ -112,10 +112,13 @@ LSGB_API int lsgb_plan_info(lsgb_plan *plan, uint32_t *kernels, uint64_t *units,
 LSGB_API void lsgb_plan_destroy(lsgb_plan *plan);
 
 /* Tuning of the mixed kernel: frequencies per thread (F), threads per CTA, the
- * minimum CTAs per SM the kernel's register budget is compiled for, the packed
- * f32x2 inner loop (1) or the scalar one (0), and two observations per loop
- * iteration (1) or one (0). 0 (-1 for the last two) keeps the current value.
- * Returns LSGB_ERR_INVALID for shapes that are not compiled in. */
+ * minimum CTAs per SM the kernel's register budget is compiled for, the inner loop
+ * (`packed`: 0 scalar rotation; 1 packed f32x2 rotation over consecutive frequencies;
+ * 2 packed f32x2 over frequencies strided by the CTA width, advanced by the
+ * second-order recurrence x[p+1] = 2 cos(phi) x[p] - x[p-1] where it is well
+ * conditioned), and two observations per loop iteration (1) or one (0). 0 (-1 for the
+ * last two) keeps the current value. Returns LSGB_ERR_INVALID for shapes that are not
+ * compiled in. */
 LSGB_API int lsgb_set_tuning(lsgb_engine *eng, int variant, int freqs_per_thread,
                              int threads_per_cta, int min_ctas_per_sm, int packed, int unroll);
 
