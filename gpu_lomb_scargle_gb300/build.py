@@ -41,7 +41,7 @@ VARIANTS = {
     "libpylserrordouble.so": ("1", "double"),
 }
 
-HEADERS = [CSRC / "lsgb_internal.h", CSRC / "lsgb_cpu.h", INCLUDE / "lsgb.h",
+HEADERS = [CSRC / "lsgb_internal.h", CSRC / "lsgb_device.h", CSRC / "lsgb_cpu.h", INCLUDE / "lsgb.h",
            INCLUDE / "lombscargle_py.h"]
 
 
@@ -78,6 +78,10 @@ def build(force: bool = False, jobs: int = 0, verbose: bool = False) -> Path:
     compile_steps.append(([nv, *ARCH, *NVCC_COMMON, "-Xptxas", "-v", "-c",
                            str(CSRC / "lsgb_kernels.cu"), "-o", str(k_obj)],
                           k_obj, [CSRC / "lsgb_kernels.cu", *HEADERS]))
+    t_obj = OBJ / "lsgb_tensor.o"
+    compile_steps.append(([nv, *ARCH, *NVCC_COMMON, "-Xptxas", "-v", "-c",
+                           str(CSRC / "lsgb_tensor.cu"), "-o", str(t_obj)],
+                          t_obj, [CSRC / "lsgb_tensor.cu", *HEADERS]))
     n_obj = OBJ / "lsgb_noalloc.o"
     compile_steps.append(([nv, *ARCH, *NVCC_COMMON, "-c", str(CSRC / "lsgb_noalloc.cu"), "-o",
                            str(n_obj)], n_obj, [CSRC / "lsgb_noalloc.cu", *HEADERS]))
@@ -101,12 +105,12 @@ def build(force: bool = False, jobs: int = 0, verbose: bool = False) -> Path:
             if verbose and log and log != "cached":
                 print(f"[{out.name}]\n{log}")
     link = [nv, *ARCH, "-shared", "-cudart", "shared", "-Xcompiler", "-fopenmp"]
-    link_steps = [(link + [str(k_obj), str(e_obj), str(n_obj), str(s_obj), "-o",
+    link_steps = [(link + [str(k_obj), str(t_obj), str(e_obj), str(n_obj), str(s_obj), "-o",
                            str(LIB / "liblsgb.so"), "-lpthread"],
-                   LIB / "liblsgb.so", [k_obj, e_obj, n_obj, s_obj])]
+                   LIB / "liblsgb.so", [k_obj, t_obj, e_obj, n_obj, s_obj])]
     for lib, o in v_objs.items():
-        link_steps.append((link + [str(o), str(k_obj), str(e_obj), "-o", str(LIB / lib)],
-                           LIB / lib, [o, k_obj, e_obj]))
+        link_steps.append((link + [str(o), str(k_obj), str(t_obj), str(e_obj), "-o", str(LIB / lib)],
+                           LIB / lib, [o, k_obj, t_obj, e_obj]))
     cli = LIB / "lsgb_main"
     link_steps.append(([nv, *NVCC_COMMON, "-O2", str(CSRC / "lsgb_cli.cpp"), "-o", str(cli), "-ldl"],
                        cli, [CSRC / "lsgb_cli.cpp"]))

@@ -1,0 +1,70 @@
+// lsgb_device.h -- device helpers shared by the CUDA-core kernels (lsgb_kernels.cu) and
+// the tensor-core kernel (lsgb_tensor.cu). Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace lsgb {
+namespace {
+
+constexpr float kTwoPiOver2p32f = 1.4629180792671596e-09f;  // 2 pi / 2^32
+
+// (power, index) ordering of the reference's argmax (source/main.cu:1545-1563):
+// larger power wins, equal power -> lower index (the first maximum).
+template <typename V>
+__device__ __forceinline__ bool better(V p1, uint32_t k1, V p2, uint32_t k2) {
+    return p1 > p2 || (p1 == p2 && k1 < k2);
+}
+
+// Standard L-S power from the sums of one frequency (N observations):
+//   P = 1/2 [ (Q+U)/(N+r) + (Q-U)/(N-r) ],  Q = XC^2+XS^2,
+//   U = [ (CC-SS)(XC^2-XS^2) + 4 CS XC XS ] / r,  r = hypot(CC-SS, 2 CS),
+// which is source/main.cu:1588-1598 with cos/sin(2 omega tau) = (CC-SS, 2CS)/r.
+// N - r is evaluated as 4 (CC SS - CS^2)/(N + r) to avoid cancellation.
+__device__ __forceinline__ float fast_sqrt(float h) { return h > 0.0f ? h * rsqrtf(h) : 0.0f; }
+
+__device__ __forceinline__ float std_power_f(float N, float xc, float xs, float cc, float cs) {
+    const float ss = N - cc;
+    const float D = cc - ss;
+    const float E = 2.0f * cs;
+    const float r = fast_sqrt(fmaf(D, D, E * E));
+    const float xc2 = xc * xc, xs2 = xs * xs;
+    const float Q = xc2 + xs2;
+    const float V = xc2 - xs2;
+    const float U = r > 0.0f ? __fdividef(fmaf(D, V, 2.0f * E * xc * xs), r) : V;
+    const float den1 = N + r;
+    const float den2 = __fdividef(4.0f * fmaf(cc, ss, -cs * cs), den1);
+    return 0.5f * (__fdividef(Q + U, den1) + __fdividef(Q - U, den2));
+}
+
+// Generalized (floating-mean) power from weighted sums with total weight W:
+// the same closed form applied to the weighted covariances, which is
+// source/main.cu:1728-1776 with the second pass expressed by rotating the
+// first-pass sums by omega*tau.
+__device__ __forceinline__ float gen_power_f(float invW, float ybar, float C, float S, float YC,
+                                             float YS, float CC, float CS) {
+    const float cb = C * invW, sb = S * invW;
+    const float cc = CC * invW, cs = CS * invW;
+    const float ss = 1.0f - cc;
+    const float yc = fmaf(-ybar, cb, YC * invW);
+    const float ys = fmaf(-ybar, sb, YS * invW);
+    const float vcc = fmaf(-cb, cb, cc);
+    const float vss = fmaf(-sb, sb, ss);
+    const float vcs = fmaf(-cb, sb, cs);
+    const float D = vcc - vss, E = 2.0f * vcs, T = vcc + vss;
+    const float r = fast_sqrt(fmaf(D, D, E * E));
+    const float yc2 = yc * yc, ys2 = ys * ys;
+    const float Q = yc2 + ys2, V = yc2 - ys2;
+    const float U = r > 0.0f ? __fdividef(fmaf(D, V, 2.0f * E * yc * ys), r) : V;
+    const float den1 = T + r;
+    const float den2 = __fdividef(4.0f * fmaf(vcc, vss, -vcs * vcs), den1);
+    return __fdividef(Q + U, den1) + __fdividef(Q - U, den2);
+}
+
+template <typename OutT>
+__device__ __forceinline__ void store_out(void *pgram, uint64_t i, float p) {
+    reinterpret_cast<OutT *>(pgram)[i] = (OutT)p;
+}
+}  // namespace
+}  // namespace lsgb

@@ -83,8 +83,11 @@ void two_prod(double a, double b_hi, double b_lo, double &hi, double &lo) {
 // Device buffers one batch needs besides the caller's arrays.
 struct Workspace {
     DevBuf objs, offs, perm, rec, tile_best, counter, keys;
+    // sticky error word of the tensor-form kernel (a bounded pipeline wait that timed
+    // out); zeroed when allocated and after it is reported
+    DevBuf status;
     void release() {
-        DevBuf *b[] = {&objs, &offs, &perm, &rec, &tile_best, &counter, &keys};
+        DevBuf *b[] = {&objs, &offs, &perm, &rec, &tile_best, &counter, &keys, &status};
         for (DevBuf *x : b) x->release();
     }
 };
@@ -178,7 +181,16 @@ int plan_batch(Batch &b, int sms, const MixedShape *shapes, uint32_t reanchor, i
     b.n_tiles = (uint32_t)n_tiles64;
     b.want_best = best_idx || best_power;
     int occ = 0;
-    if (mixed) {
+    if (mixed && b.shape.x2 == 3) {
+        // tensor form: one persistent CTA per SM with its own shared-memory ring
+        if ((uint32_t)b.shape.f * (uint32_t)b.shape.nt != tensor_tile_freqs(variant))
+            return fail(LSGB_ERR_INVALID, "tensor form: shape %dx%d is not compiled", b.shape.f,
+                        b.shape.nt);
+        b.chunk = 0;
+        b.fold = false;
+        b.smem = tensor_smem_bytes(variant);
+        occ = 1;
+    } else if (mixed) {
         // Shared memory per CTA: at most what keeps the CTAs per SM that the shape's
         // register budget allows resident (less the per-CTA reservation and the static
         // variables), and at most kMixedSmemMax of staged records.
@@ -221,6 +233,10 @@ int upload_tables(const Batch &b, Workspace &ws, cudaStream_t st) {
     if (b.want_best && !mixed) LSGB_CUDA(ws.tile_best.ensure(sizeof(TileBest) * b.units));
     if (b.want_best && mixed) LSGB_CUDA(ws.keys.ensure(sizeof(unsigned long long) * b.n_obj));
     if (mixed) LSGB_CUDA(ws.rec.ensure(mixed_global_rec_bytes(b.shape) * b.rows));
+    if (mixed && !ws.status.p) {
+        LSGB_CUDA(ws.status.ensure(sizeof(uint32_t)));
+        LSGB_CUDA(cudaMemsetAsync(ws.status.p, 0, sizeof(uint32_t), st));
+    }
     LSGB_CUDA(cudaMemcpyAsync(ws.objs.p, b.objs.data(), sizeof(ObjInfo) * b.n_obj,
                               cudaMemcpyHostToDevice, st));
     LSGB_CUDA(cudaMemcpyAsync(ws.offs.p, b.offsets.data(), sizeof(uint64_t) * (b.n_obj + 1),
@@ -228,6 +244,18 @@ int upload_tables(const Batch &b, Workspace &ws, cudaStream_t st) {
     LSGB_CUDA(cudaMemcpyAsync(ws.perm.p, b.perm.data(), sizeof(uint32_t) * b.n_obj,
                               cudaMemcpyHostToDevice, st));
     return LSGB_OK;
+}
+
+// Reports (and clears) a pipeline-wait timeout recorded by the tensor-form kernel. Call
+// after the work that may have set it has completed.
+int check_status(Workspace &ws) {
+    if (!ws.status.p) return LSGB_OK;
+    uint32_t v = 0;
+    LSGB_CUDA(cudaMemcpy(&v, ws.status.p, sizeof(v), cudaMemcpyDeviceToHost));
+    if (v == 0) return LSGB_OK;
+    LSGB_CUDA(cudaMemset(ws.status.p, 0, sizeof(uint32_t)));
+    return fail(LSGB_ERR_CUDA,
+                "tensor-form kernel: a pipeline wait timed out; the results of the call are invalid");
 }
 
 // Records `ev` on `st`; while `st` is being captured the record becomes an event node
@@ -272,6 +300,7 @@ int enqueue_batch(Batch &b, Workspace &ws, cudaStream_t st, cudaEvent_t ev0, cud
         a.best_key = b.want_best ? (unsigned long long *)ws.keys.p : nullptr;
         a.reanchor = b.reanchor;
         a.fold = b.fold ? 1u : 0u;
+        a.status = (uint32_t *)ws.status.p;
         if (ev0) LSGB_CUDA(record(ev0, st, capturing));
         LSGB_CUDA(launch_mixed(b.variant, b.dtype, b.shape, a, b.grid, b.smem, st));
         if (ev1) LSGB_CUDA(record(ev1, st, capturing));
@@ -400,7 +429,7 @@ LSGB_API int lsgb_set_tuning(lsgb_engine *eng, int variant, int f, int nt, int m
     if (f > 0) s.f = f;
     if (nt > 0) s.nt = nt;
     if (minb > 0) s.minb = minb;
-    if (x2 >= 0) s.x2 = x2 > 2 ? -1 : x2;  // -1 matches no compiled shape
+    if (x2 >= 0) s.x2 = x2 > 3 ? -1 : x2;  // -1 matches no compiled shape
     if (unroll >= 0) s.uj = unroll ? 1 : 0;
     int blocks = 0;
     if (mixed_occupancy(variant, LSGB_F32, s, 1024, &blocks) != cudaSuccess)
@@ -457,7 +486,7 @@ LSGB_API int lsgb_last_kernel_time(lsgb_engine *eng, float *ms) {
     if (!eng->ev_valid) return fail(LSGB_ERR_INVALID, "no main kernel has been launched");
     LSGB_CUDA(cudaEventSynchronize(eng->ev_main1));
     LSGB_CUDA(cudaEventElapsedTime(ms, eng->ev_main0, eng->ev_main1));
-    return LSGB_OK;
+    return check_status(eng->ws);
 }
 
 LSGB_API int lsgb_periodogram_device(lsgb_engine *eng, int variant, int precision, int dtype,
@@ -673,7 +702,7 @@ LSGB_API int lsgb_periodogram_host(lsgb_engine *eng, int variant, int precision,
             LSGB_CUDA(cudaMemcpyAsync(best_idx, d_idx, sizeof(uint32_t) * n_obj, cudaMemcpyDeviceToHost, st));
         if (d_p) LSGB_CUDA(cudaMemcpyAsync(best_power, d_p, es * n_obj, cudaMemcpyDeviceToHost, st));
         LSGB_CUDA(cudaStreamSynchronize(st));
-        return LSGB_OK;
+        return check_status(eng->ws);
     }
     int rc = lsgb_periodogram_device(eng, variant, precision, dtype, eng->in_t.p, eng->in_y.p, d_dy,
                                      offsets, n_obj, fmin, df, n_freq, normalize, d_pg, d_idx, d_p,
@@ -694,7 +723,7 @@ LSGB_API int lsgb_periodogram_host(lsgb_engine *eng, int variant, int precision,
         LSGB_CUDA(cudaMemcpyAsync(best_idx, d_idx, sizeof(uint32_t) * n_obj, cudaMemcpyDeviceToHost, st));
     if (d_p) LSGB_CUDA(cudaMemcpyAsync(best_power, d_p, es * n_obj, cudaMemcpyDeviceToHost, st));
     LSGB_CUDA(cudaStreamSynchronize(st));
-    return LSGB_OK;
+    return check_status(eng->ws);
 }
 
 }  // extern "C"

@@ -88,6 +88,8 @@ struct MixedArgs {
                                    // null to use tile_best; zero means "no positive power"
     uint32_t fold;         // 1: shared memory holds a second-level sum area after the records
                            // (objects longer than `chunk` fold their chunk sums into it)
+    uint32_t *status;      // tensor form: bit 0 set when a bounded pipeline wait timed out
+                           // (may be null)
 };
 
 
@@ -108,7 +110,8 @@ struct MixedShape {
     int f, nt, minb;
     int x2;  // 0: scalar loop; 1: packed f32x2 loop (two interleaved frequency chains per
              // thread, rotation steps); 2: packed loop with strided frequencies and
-             // second-order recurrence steps (SoRec records)
+             // second-order recurrence steps (SoRec records); 3: tensor-core form
+             // (lsgb_tensor.cu; f = coarse steps per unit, nt = 128 fine steps)
     int uj;  // 1: two observations per inner-loop iteration (independent chains), 0: one
 };
 // Bytes of shared memory per staged observation of a mixed shape.
@@ -133,6 +136,12 @@ cudaError_t launch_records(int variant, int dtype, const void *t, const void *y,
 cudaError_t launch_mixed(int variant, int dtype, MixedShape shape, const MixedArgs &a,
                          int grid, size_t smem, cudaStream_t st);
 cudaError_t mixed_occupancy(int variant, int dtype, MixedShape shape, size_t smem, int *blocks);
+// Tensor-core form (lsgb_tensor.cu): frequencies per work unit, dynamic shared memory,
+// launch (one persistent CTA per SM, grid <= SMs; MixedArgs as for the mixed kernel,
+// ObsRec records).
+uint32_t tensor_tile_freqs(int variant);
+size_t tensor_smem_bytes(int variant);
+cudaError_t launch_tensor(int variant, int dtype, const MixedArgs &a, int grid, cudaStream_t st);
 // Compiled mixed shapes as (variant, F, threads, min CTAs, packed, unroll); returns the count.
 int mixed_shapes(int *out, int max_shapes);
 cudaError_t launch_plain(int variant, int in_dtype, int out_dtype, const PlainArgs &a, int grid,

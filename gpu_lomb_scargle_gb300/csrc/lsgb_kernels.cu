@@ -24,6 +24,7 @@
 #include <math.h>
 #include <stdint.h>
 
+#include "lsgb_device.h"
 #include "lsgb_internal.h"
 
 namespace lsgb {
@@ -31,7 +32,6 @@ namespace lsgb {
 namespace {
 
 constexpr double kTwoPiOver2p64 = 3.4061215800865545e-19;  // 2 pi / 2^64
-constexpr float kTwoPiOver2p32f = 1.4629180792671596e-09f;  // 2 pi / 2^32
 constexpr double k2p64 = 18446744073709551616.0;
 
 template <typename T>
@@ -73,13 +73,6 @@ __device__ __forceinline__ uint64_t frac_turns_u64(double x_hi, double x_lo, dou
     const uint64_t u = __double2ull_rz(r_hi * k2p64);
     const long long e = __double2ll_rn(p_lo * k2p64);
     return u + (uint64_t)e;
-}
-
-// (power, index) ordering of the reference's argmax (source/main.cu:1545-1563):
-// larger power wins, equal power -> lower index (the first maximum).
-template <typename V>
-__device__ __forceinline__ bool better(V p1, uint32_t k1, V p2, uint32_t k2) {
-    return p1 > p2 || (p1 == p2 && k1 < k2);
 }
 
 template <int NT, typename V>
@@ -244,55 +237,6 @@ __global__ void records_kernel(int variant, int dtype, const void *t, const void
 // Mixed kernel.
 // ---------------------------------------------------------------------------
 
-// Standard L-S power from the sums of one frequency (N observations):
-//   P = 1/2 [ (Q+U)/(N+r) + (Q-U)/(N-r) ],  Q = XC^2+XS^2,
-//   U = [ (CC-SS)(XC^2-XS^2) + 4 CS XC XS ] / r,  r = hypot(CC-SS, 2 CS),
-// which is source/main.cu:1588-1598 with cos/sin(2 omega tau) = (CC-SS, 2CS)/r.
-// N - r is evaluated as 4 (CC SS - CS^2)/(N + r) to avoid cancellation.
-__device__ __forceinline__ float fast_sqrt(float h) { return h > 0.0f ? h * rsqrtf(h) : 0.0f; }
-
-__device__ __forceinline__ float std_power_f(float N, float xc, float xs, float cc, float cs) {
-    const float ss = N - cc;
-    const float D = cc - ss;
-    const float E = 2.0f * cs;
-    const float r = fast_sqrt(fmaf(D, D, E * E));
-    const float xc2 = xc * xc, xs2 = xs * xs;
-    const float Q = xc2 + xs2;
-    const float V = xc2 - xs2;
-    const float U = r > 0.0f ? __fdividef(fmaf(D, V, 2.0f * E * xc * xs), r) : V;
-    const float den1 = N + r;
-    const float den2 = __fdividef(4.0f * fmaf(cc, ss, -cs * cs), den1);
-    return 0.5f * (__fdividef(Q + U, den1) + __fdividef(Q - U, den2));
-}
-
-// Generalized (floating-mean) power from weighted sums with total weight W:
-// the same closed form applied to the weighted covariances, which is
-// source/main.cu:1728-1776 with the second pass expressed by rotating the
-// first-pass sums by omega*tau.
-__device__ __forceinline__ float gen_power_f(float invW, float ybar, float C, float S, float YC,
-                                             float YS, float CC, float CS) {
-    const float cb = C * invW, sb = S * invW;
-    const float cc = CC * invW, cs = CS * invW;
-    const float ss = 1.0f - cc;
-    const float yc = fmaf(-ybar, cb, YC * invW);
-    const float ys = fmaf(-ybar, sb, YS * invW);
-    const float vcc = fmaf(-cb, cb, cc);
-    const float vss = fmaf(-sb, sb, ss);
-    const float vcs = fmaf(-cb, sb, cs);
-    const float D = vcc - vss, E = 2.0f * vcs, T = vcc + vss;
-    const float r = fast_sqrt(fmaf(D, D, E * E));
-    const float yc2 = yc * yc, ys2 = ys * ys;
-    const float Q = yc2 + ys2, V = yc2 - ys2;
-    const float U = r > 0.0f ? __fdividef(fmaf(D, V, 2.0f * E * yc * ys), r) : V;
-    const float den1 = T + r;
-    const float den2 = __fdividef(4.0f * fmaf(vcc, vss, -vcs * vcs), den1);
-    return __fdividef(Q + U, den1) + __fdividef(Q - U, den2);
-}
-
-template <typename OutT>
-__device__ __forceinline__ void store_out(void *pgram, uint64_t i, float p) {
-    reinterpret_cast<OutT *>(pgram)[i] = (OutT)p;
-}
 template <typename OutT>
 __device__ __forceinline__ void store_out_d(void *pgram, uint64_t i, double p) {
     reinterpret_cast<OutT *>(pgram)[i] = (OutT)p;
@@ -1026,6 +970,12 @@ cudaError_t launch_records(int variant, int dtype, const void *t, const void *y,
 
 cudaError_t launch_mixed(int variant, int dtype, MixedShape shape, const MixedArgs &a, int grid,
                          size_t smem, cudaStream_t st) {
+    if (shape.x2 == 3) {
+        if ((uint32_t)shape.f * (uint32_t)shape.nt != tensor_tile_freqs(variant) || shape.minb != 1 ||
+            shape.uj || a.reanchor)
+            return cudaErrorInvalidValue;
+        return launch_tensor(variant, dtype, a, grid, st);
+    }
 #define X(F_, NT_, MB_, G_, PK_, UJ_, RA_)                                           \
     if (shape.f == F_ && shape.nt == NT_ && shape.minb == MB_ && (variant == 1) == G_ && \
         shape.x2 == PK_ && (shape.uj ? 2 : 1) == UJ_ && (a.reanchor != 0) == RA_)        \
@@ -1050,10 +1000,29 @@ int mixed_shapes(int *out, int max_shapes) {
     n += RA_ ? 0 : 1;
     LSGB_MIXED_SHAPES(X)
 #undef X
+    // the tensor-core form of each variant: (coarse steps per unit, 128 fine steps)
+    for (int v = 0; v < 2; ++v) {
+        if (out && n < max_shapes) {
+            out[6 * n + 0] = v;
+            out[6 * n + 1] = (int)(tensor_tile_freqs(v) / 128u);
+            out[6 * n + 2] = 128;
+            out[6 * n + 3] = 1;
+            out[6 * n + 4] = 3;
+            out[6 * n + 5] = 0;
+        }
+        ++n;
+    }
     return n;
 }
 
 cudaError_t mixed_occupancy(int variant, int dtype, MixedShape shape, size_t smem, int *blocks) {
+    if (shape.x2 == 3) {
+        if ((uint32_t)shape.f * (uint32_t)shape.nt != tensor_tile_freqs(variant) || shape.minb != 1 ||
+            shape.uj)
+            return cudaErrorInvalidValue;
+        *blocks = 1;
+        return cudaSuccess;
+    }
 #define X(F_, NT_, MB_, G_, PK_, UJ_, RA_)                                           \
     if (shape.f == F_ && shape.nt == NT_ && shape.minb == MB_ && (variant == 1) == G_ && \
         shape.x2 == PK_ && (shape.uj ? 2 : 1) == UJ_ && !RA_)                            \
