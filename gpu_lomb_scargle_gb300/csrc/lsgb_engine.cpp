@@ -284,7 +284,8 @@ int enqueue_batch(Batch &b, Workspace &ws, cudaStream_t st, cudaEvent_t ev0, cud
         two_prod(b.df, kInv2PiHi, kInv2PiLo, g.df_hi, g.df_lo);
         LSGB_CUDA(launch_records(b.variant, b.dtype, b.t, b.y, b.dy, (const uint64_t *)ws.offs.p,
                                  b.n_obj, d_objs, b.rows, g, ws.rec.p,
-                                 b.shape.x2 == 2 ? (uint32_t)b.shape.nt : 0u, st));
+                                 b.shape.x2 == 2 ? (uint32_t)b.shape.nt : 0u,
+                                 b.shape.x2 == 3 ? kTensorRowStep : 1u, st));
         ++kernels;
         MixedArgs a{};
         a.rec = ws.rec.p;
@@ -353,9 +354,9 @@ struct lsgb_engine {
     cudaStream_t d2h = nullptr;     // host-buffer API: periodogram copies overlapping compute
     Workspace ws;
     DevBuf in_t, in_y, in_dy, out_pg, out_idx, out_p;
-    // defaults measured fastest on the 999-object, 1e6-frequency batches: the strided
-    // second-order loop for both variants
-    MixedShape shape[2] = {{12, 256, 2, 2, 0}, {10, 256, 2, 2, 0}};
+    // defaults measured fastest on the 999-object, 1e6-frequency batches: the tensor-core
+    // form (lsgb_tensor.cu) for both variants
+    MixedShape shape[2] = {{32, 128, 1, 3, 0}, {16, 128, 1, 3, 0}};
     uint32_t last_kernels = 0;
     uint64_t last_units = 0;
     cudaEvent_t ev_main0 = nullptr, ev_main1 = nullptr;  // around the last main-kernel launch

@@ -11,7 +11,8 @@ namespace lsgb {
 //   a = frac(f0 * t)  and  b = frac(dfturn * t)  in units of 2^-64 turns, where
 //   f0 = fmin / 2pi and dfturn = df / 2pi, so the phase of grid point k is
 //   a + k*b (mod 2^64), exact to ~(1+k) * 2^-64 turns;
-//   cd, sd = cos, sin(2 pi b): the per-step rotation of the recurrence;
+//   cd, sd = cos, sin(2 pi s b): the rotation by s grid points (s = 1 for the
+//   recurrence loops, kTensorRowStep for the tensor form);
 //   standard:    v0 = y,          v1 = 0
 //   generalized: v0 = w / W,      v1 = (w / W) * (y - ybar_w),   w = 1/dy^2.
 struct __align__(16) ObsRec {
@@ -59,6 +60,9 @@ struct ObjInfo {
     float invw32;   // (float)(1 / wsum_f)
     float ybar32;   // (float)ybar_f
     float pad32;
+    // tensor form: powers of two that bring the largest |v0| / |v1| of the object's
+    // records into (1/2, 1] (FP16 operands); 1 when the weights are all zero
+    float tsc0, tsc1;
 };
 
 // Best (power, index) of one (object, frequency tile).
@@ -126,12 +130,17 @@ inline size_t mixed_fold_bytes(int variant, const MixedShape &s) {
 // ---- launchers (lsgb_kernels.cu); all asynchronous on `st` ----
 cudaError_t launch_stats(int variant, int mixed, int dtype, int normalize, const void *y,
                          const void *dy, ObjInfo *objs, uint32_t n_obj, cudaStream_t st);
-// so_stride 0: ObsRec records; > 0: SoRec records for a second-order shape whose CTA
-// has so_stride threads. `rec` holds rows x 32 or rows x 96 bytes accordingly.
+// so_stride 0: ObsRec records whose (cd, sd) step is obs_step grid points (1 for the
+// rotation loops, kTensorRowStep for the tensor form); > 0: SoRec records for a
+// second-order shape whose CTA has so_stride threads. `rec` holds rows x 32 or rows x 96
+// bytes accordingly.
 cudaError_t launch_records(int variant, int dtype, const void *t, const void *y, const void *dy,
                            const uint64_t *offsets, uint32_t n_obj, const ObjInfo *objs,
                            uint64_t rows, GridTurns g, void *rec, uint32_t so_stride,
-                           cudaStream_t st);
+                           uint32_t obs_step, cudaStream_t st);
+// Grid-point distance of the two A rows a tensor-form producer thread computes (the second
+// by rotating the first with the record's (cd, sd)).
+constexpr uint32_t kTensorRowStep = 8;
 // Mixed kernel: returns cudaErrorInvalidValue when (variant, dtype, shape) is not compiled.
 cudaError_t launch_mixed(int variant, int dtype, MixedShape shape, const MixedArgs &a,
                          int grid, size_t smem, cudaStream_t st);

@@ -106,6 +106,33 @@ __device__ __forceinline__ void block_best(V &bp, uint32_t &bk, V *s_p, uint32_t
 //            quantities the mixed kernel needs to undo the float rounding of
 //            the stored weights.
 // ---------------------------------------------------------------------------
+// Block-wide maximum of non-negative doubles (blockDim.x a multiple of 32, <= 1024).
+__device__ double block_max(double v, double *s_red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) s_red[w] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (w == 0) {
+        r = (l < (int)(blockDim.x >> 5)) ? s_red[l] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r = fmax(r, __shfl_xor_sync(0xffffffffu, r, o));
+        if (l == 0) s_red[0] = r;
+    }
+    __syncthreads();
+    return s_red[0];
+}
+
+// The power of two 2^-e with m / 2^e in (1/2, 1] (1 for m == 0).
+__device__ float pow2_scale(double m) {
+    if (!(m > 0.0) || !isfinite(m)) return 1.0f;
+    int e;
+    frexp(m, &e);  // m = f 2^e, f in [1/2, 1)
+    return (float)ldexp(1.0, -e);
+}
+
 __global__ void stats_kernel(int variant, int mixed, int dtype, int normalize, const void *y,
                              const void *dy, ObjInfo *objs) {
     __shared__ double s_red[32];
@@ -122,10 +149,18 @@ __global__ void stats_kernel(int variant, int mixed, int dtype, int normalize, c
             s2 += d * d;
         }
         s2 = block_sum(s2, s_red);
+        double ym = 0.0;
+        if (mixed) {
+            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+                ym = fmax(ym, fabs((double)(float)load_in(dtype, y, r0 + i)));
+            ym = block_max(ym, s_red);
+        }
         if (threadIdx.x == 0) {
             const double sigma = sqrt(s2 / (n * 1.0));
             ob.norm = normalize ? 2.0 / (n * (sigma * sigma)) : 1.0;
             ob.norm32 = (float)ob.norm;
+            ob.tsc0 = pow2_scale(ym);
+            ob.tsc1 = 1.0f;
         }
         return;
     }
@@ -145,7 +180,7 @@ __global__ void stats_kernel(int variant, int mixed, int dtype, int normalize, c
     }
     const double W = block_sum(w_s, s_red);
     const double ym = block_sum(wy_s, s_red) / W;
-    double wf_s = 0.0, yf_s = 0.0, yy_s = 0.0;
+    double wf_s = 0.0, yf_s = 0.0, yy_s = 0.0, m0 = 0.0, m1 = 0.0;
     for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
         double w = 1.0 / load_in(dtype, dy, r0 + i);
         w = w * w;
@@ -154,10 +189,14 @@ __global__ void stats_kernel(int variant, int mixed, int dtype, int normalize, c
         wf_s += (double)(float)wn;
         yf_s += (double)(float)(wn * yc);
         yy_s += wn * yc * yc;
+        m0 = fmax(m0, (double)(float)wn);
+        m1 = fmax(m1, fabs((double)(float)(wn * yc)));
     }
     const double wf = block_sum(wf_s, s_red);
     const double yf = block_sum(yf_s, s_red);
     const double yy = block_sum(yy_s, s_red);
+    m0 = block_max(m0, s_red);
+    m1 = block_max(m1, s_red);
     if (threadIdx.x == 0) {
         ob.wtot = W;
         ob.ymean = ym;
@@ -168,6 +207,8 @@ __global__ void stats_kernel(int variant, int mixed, int dtype, int normalize, c
         ob.norm32 = (float)ob.norm;
         ob.invw32 = (float)(1.0 / wf);
         ob.ybar32 = (float)ybar;
+        ob.tsc0 = pow2_scale(m0);
+        ob.tsc1 = pow2_scale(m1);
     }
 }
 
@@ -177,7 +218,7 @@ __global__ void stats_kernel(int variant, int mixed, int dtype, int normalize, c
 __global__ void records_kernel(int variant, int dtype, const void *t, const void *y,
                                const void *dy, const uint64_t *offsets, uint32_t n_obj,
                                const ObjInfo *objs, uint64_t rows, GridTurns g, void *rec,
-                               uint32_t so_stride) {
+                               uint32_t so_stride, uint32_t obs_step) {
     for (uint64_t row = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; row < rows;
          row += (uint64_t)gridDim.x * blockDim.x) {
         const double td = load_in(dtype, t, row);
@@ -185,7 +226,7 @@ __global__ void records_kernel(int variant, int dtype, const void *t, const void
         const uint64_t b = frac_turns_u64(g.df_hi, g.df_lo, td);
         // the step of the recurrence: one grid point, or so_stride of them (exact in the
         // fixed-point turns; the signed reading puts the angle in [-pi, pi))
-        const uint64_t bs = so_stride ? b * (uint64_t)so_stride : b;
+        const uint64_t bs = b * (uint64_t)(so_stride ? so_stride : obs_step);
         double sd, cd;
         sincos((double)(long long)bs * kTwoPiOver2p64, &sd, &cd);
         ObsRec r;
@@ -959,12 +1000,12 @@ cudaError_t launch_stats(int variant, int mixed, int dtype, int normalize, const
 cudaError_t launch_records(int variant, int dtype, const void *t, const void *y, const void *dy,
                            const uint64_t *offsets, uint32_t n_obj, const ObjInfo *objs,
                            uint64_t rows, GridTurns g, void *rec, uint32_t so_stride,
-                           cudaStream_t st) {
+                           uint32_t obs_step, cudaStream_t st) {
     if (rows == 0) return cudaSuccess;
     const uint64_t blocks64 = (rows + 255) / 256;
     const int blocks = (int)(blocks64 < 65535ull * 16 ? blocks64 : 65535ull * 16);
     records_kernel<<<blocks, 256, 0, st>>>(variant, dtype, t, y, dy, offsets, n_obj, objs, rows, g,
-                                           rec, so_stride);
+                                           rec, so_stride, obs_step ? obs_step : 1u);
     return cudaGetLastError();
 }
 

@@ -1,4 +1,5 @@
-// lsgb_tensor.cu -- the tensor-core form of the mixed periodogram (sm_103a: tcgen05, TMEM).
+// lsgb_tensor.cu -- the tensor-core form of the mixed periodogram (sm_103a: tcgen05, TMEM,
+// bulk copies).
 //
 // The sums of the hot loop (source/kernel.cu:484-631 standard, :368-477 generalized) are
 // recast as small complex matrix products. Within one work unit (object o, frequencies
@@ -7,24 +8,37 @@
 // so with A[p][j] = v_j exp(i alpha_jp) and B[m][j] = exp(i m beta_j)
 //   sum_j v_j exp(i theta_jk) = (A B^T)[p][m],
 // and the squared terms follow from the doubled angle, cos^2 = (1 + cos 2theta) / 2,
-// cos sin = sin 2theta / 2, with A2 = exp(2i alpha), B2 = exp(2i m beta). Both angles
-// come from the exact 64-bit fixed-point phases of ObsRec (a + k b mod 2^64 turns).
+// cos sin = sin 2theta / 2, with A2 = exp(2i alpha) (times v for the generalized variant)
+// and B2 = exp(2i m beta). Both angles come from the exact 64-bit fixed-point phases of
+// ObsRec (a + k b mod 2^64 turns).
 //
-// Each complex product is two real MMAs with N = 2 NM: [XC | XS] = Ar [Br | Bi]^T +
+// Each complex product is two real MMAs with N = 2 NM: [Re | Im] = Ar [Br | Bi]^T +
 // Ai [-Bi | Br]^T, the right factors being two overlapping row windows of
-// Z = [-Bi; Br; Bi]. FP32 accuracy on the TF32 tensor cores comes from the split
-// x = hi + lo (hi = x rounded to TF32, lo = x - hi): a b ~ ah bh + ah bl + al bh
-// (the dropped al bl is below 2^-21 relative).
+// Z = [-Bi; Br; Bi]. FP32 accuracy on the FP16 tensor cores comes from the split
+// x = hi + lo (hi: x to 11 significant bits by Veltkamp's method, lo = x - hi rounded to
+// FP16), a b ~ ah bh + ah bl + al bh: every operand is a cosine or sine times a weight
+// scaled into [-1, 1] by a power of two per object (ObjInfo::tsc0/tsc1), so hi + lo
+// carries x to about 2^-24 (lo may be subnormal, whose absolute spacing is 2^-24).
+//
+// The tensor cores round their FP32 accumulations toward zero, which makes the error of
+// a long accumulation grow linearly with its length. So a unit's observations are summed
+// in passes of kPassKB K-blocks into one of two TMEM partial buffers, and the epilogue
+// warps fold each finished pass into an FP32 running sum in TMEM with round-to-nearest
+// adds; the last pass of a unit is folded straight into the power computation.
 //
 // One persistent CTA per SM, warp-specialized:
-//   warps 0-3   epilogue: read the accumulators from TMEM (warp w owns lanes 32w..),
-//               power per frequency, periodogram store, per-object maximum;
+//   warps 0-3   fold and epilogue: TMEM lanes 32w.. (the lanes warp w may access), power
+//               per frequency, periodogram store, per-object maximum;
 //   warp 4      TMEM allocation and the MMA issuer (one thread);
-//   warps 5-12  producers: the split operands of 8 observations (one K-block) per stage
-//               of a shared-memory ring, in the K-major no-swizzle layout.
-// Shared-memory stages and the two TMEM accumulator buffers are handed over with
-// mbarriers. Every wait is bounded: on a timeout the kernel records an error in
-// MixedArgs::status, lets its issued MMAs drain, frees its TMEM and returns.
+//   warp 5      record loader (one thread): bulk copies of 16 ObsRec per K-block into a
+//               shared-memory ring;
+//   warps 6-13  producers: the split FP16 operands of one K-block (16 observations) per
+//               stage of a shared-memory ring, K-major without swizzle. A thread computes
+//               A rows p and p + kTensorRowStep, the second by rotating the first with
+//               the record's (cd, sd), so half the A entries need no SFU sine/cosine.
+// All hand-offs use mbarriers. Every wait is bounded: on a timeout the kernel records an
+// error in MixedArgs::status, lets its issued MMAs drain, frees its TMEM and returns.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -36,40 +50,46 @@ namespace lsgb {
 namespace {
 
 constexpr int kTP = 128;        // fine frequency offsets p: A rows, TMEM lanes
-constexpr int kTK = 8;          // observations per K-block (the TF32 MMA depth)
-constexpr int kStages = 3;      // shared-memory ring depth
-constexpr int kThreads = 416;   // 13 warps
+constexpr int kTK = 16;         // observations per K-block (the FP16 MMA depth)
+constexpr int kPassKB = 4;      // K-blocks accumulated in TMEM before an FP32 fold
+constexpr int kRecSlots = 8;    // record ring depth (K-blocks)
+constexpr int kRecSlotBytes = kTK * 32;
+constexpr int kThreads = 448;   // 14 warps
+constexpr int kProducerWarp0 = 6;
 constexpr int kProducerThreads = 256;
 constexpr int kEpilogueThreads = 128;
 constexpr uint32_t kTmemCols = 512;
-constexpr uint32_t kBufCols = 256;  // TMEM columns of one accumulator buffer
+constexpr uint32_t kBufCols = 128;   // TMEM columns of one partial buffer
+constexpr uint32_t kRunCol = 256;    // first TMEM column of the running sums
 constexpr long long kWaitCycles = 1ll << 32;  // ~2 s at 2 GHz
 
 // Per-variant geometry.
 template <bool GEN>
 struct TGeo {
-    static constexpr int NM = GEN ? 32 : 64;       // coarse frequency steps m per unit
+    static constexpr int NM = GEN ? 16 : 32;       // coarse frequency steps m per unit
     static constexpr int N = 2 * NM;               // MMA N: [real | imaginary]
-    static constexpr int NAG = GEN ? 3 : 2;        // A groups: v e^ia (, v1 e^ia), e^2ia
-    static constexpr int A_BYTES = kTP * kTK * 4;  // one 128 x 8 TF32 matrix
+    static constexpr int NAG = GEN ? 3 : 2;        // A groups: v e^ia (, v1 e^ia), (v) e^2ia
+    static constexpr int W = NAG * N;              // accumulator columns per unit
+    static constexpr int A_BYTES = kTP * kTK * 2;  // one 128 x 16 FP16 matrix
     static constexpr int Z_ROWS = 3 * NM;
-    static constexpr int Z_BYTES = Z_ROWS * kTK * 4;
-    // stage: A matrices (group g, part re/im, hi/lo) then Z matrices (angle 1/2, hi/lo)
-    static constexpr int A_OFF = 0;
+    static constexpr int Z_BYTES = Z_ROWS * kTK * 2;
+    // stage: A matrices (group g, re/im, hi/lo) then Z matrices (angle 1/2, hi/lo)
     static constexpr int Z_OFF = NAG * 4 * A_BYTES;
     static constexpr int STAGE = ((Z_OFF + 4 * Z_BYTES) + 1023) / 1024 * 1024;
+    static constexpr int STAGES = GEN ? 3 : 4;
     static constexpr int TILE = kTP * NM;          // frequencies per unit
+    static_assert(W <= (int)kBufCols, "partial buffer too narrow");
 };
-
-// Byte offset of element (row r, column k < 8) of a K-major, no-swizzle operand:
-// 8-row x 16-byte core matrices, the two K halves 128 bytes apart (LBO), row groups
-// 256 bytes apart (SBO).
-__device__ __forceinline__ uint32_t kmaj_off(uint32_t r, uint32_t k) {
-    return (r & 7u) * 16u + (r >> 3) * 256u + (k & 3u) * 4u + (k >> 2) * 128u;
-}
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Byte offset of element (row r, column k < 16) of a K-major, no-swizzle FP16 operand:
+// 8-row x 16-byte core matrices, the two K halves 128 bytes apart (LBO), row groups
+// 256 bytes apart (SBO).
+__device__ __forceinline__ uint32_t kmaj_off(uint32_t r, uint32_t k) {
+    return (r & 7u) * 16u + (r >> 3) * 256u + (k & 7u) * 2u + (k >> 3) * 128u;
 }
 
 // Shared-memory matrix descriptor (tcgen05): start address, LBO, SBO in 16-byte units,
@@ -79,17 +99,24 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
            ((uint64_t)(256u >> 4) << 32) | (1ull << 46);
 }
 
-// Instruction descriptor of kind::tf32, FP32 accumulator, K-major A and B.
-__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
-    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) |
-           ((uint32_t)(M >> 4) << 24);
+// Instruction descriptor of kind::f16 with FP16 A and B, FP32 accumulator, K-major.
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
+    return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-__device__ __forceinline__ void split_tf32(float x, uint32_t &hi, uint32_t &lo) {
-    uint32_t h;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
-    hi = h;
-    lo = __float_as_uint(x - __uint_as_float(h));
+// Veltkamp's split of an FP32 value (|x| <= 1) into hi with 11 significant bits (exact in
+// FP16 down to 2^-14) and lo = x - hi (exact in FP32; its FP16 rounding costs at most
+// 2^-25 absolute). Four FP32 operations, no conversions.
+__device__ __forceinline__ void vsplit(float x, float &hi, float &lo) {
+    const float t = __fmul_rn(x, 8193.0f);  // 2^13 + 1
+    hi = __fsub_rn(t, __fsub_rn(t, x));
+    lo = __fsub_rn(x, hi);
+}
+
+// Two FP32 values as one packed FP16 pair (first value in the low half).
+__device__ __forceinline__ uint32_t pack_h2(float a, float b) {
+    const __half2 h = __floats2half2_rn(a, b);
+    return *reinterpret_cast<const uint32_t *>(&h);
 }
 
 __device__ __forceinline__ void mbar_init(uint64_t *b, uint32_t count) {
@@ -97,6 +124,11 @@ __device__ __forceinline__ void mbar_init(uint64_t *b, uint32_t count) {
 }
 __device__ __forceinline__ void mbar_arrive(uint64_t *b) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)),
+                 "r"(bytes)
+                 : "memory");
 }
 __device__ __forceinline__ bool mbar_test(uint64_t *b, uint32_t parity) {
     uint32_t done;
@@ -128,11 +160,20 @@ __device__ __noinline__ bool mbar_wait(uint64_t *b, uint32_t parity, volatile ui
     }
 }
 
-__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
-                                         uint32_t accumulate) {
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes,
+                                              uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(__cvta_generic_to_global(src)), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                        uint32_t accumulate) {
     asm volatile(
         "{ .reg .pred p; setp.ne.b32 p, %4, 0; "
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p; }" ::"r"(d_tmem),
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }" ::"r"(d_tmem),
         "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
         : "memory");
 }
@@ -148,30 +189,36 @@ __device__ __forceinline__ void tc_fence_before() {
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
 }
 
-// 16 consecutive accumulator columns of this thread's TMEM lane.
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-    uint32_t r[16];
+// 8 consecutive accumulator columns of this thread's TMEM lane (asynchronous until
+// tmem_wait_ld).
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                   "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const float (&v)[8]) {
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
-        "%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-          "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+        "tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr),
+        "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+        "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+        "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
+        : "memory");
 }
 __device__ __forceinline__ void tmem_wait_ld() {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
+__device__ __forceinline__ void tmem_wait_st() {
+    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
 
-// Phase of fixed-point turn count x as (sin, cos) on the SFU.
+// Sine and cosine of a 32-bit fixed-point turn count, on the SFU.
 __device__ __forceinline__ void turn_sincos(uint32_t hi, float &s, float &c) {
     __sincosf((float)(int32_t)hi * kTwoPiOver2p32f, &s, &c);
 }
 
 struct UnitInfo {
-    uint32_t o, tile, n;
+    uint32_t o, tile, n, nkb;
     uint64_t row0;
 };
 
@@ -182,18 +229,21 @@ __device__ __forceinline__ UnitInfo unit_info(const MixedArgs &a, uint32_t u) {
     w.tile = u - oi * a.n_tiles;
     w.row0 = a.objs[w.o].row0;
     w.n = a.objs[w.o].n;
+    w.nkb = (w.n + kTK - 1) / kTK;
     return w;
 }
 
 template <bool GEN, typename OutT>
 __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
     using G = TGeo<GEN>;
+    constexpr int S = G::STAGES;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    // 1024-byte aligned ring of stages
     unsigned char *ring = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    __shared__ __align__(8) uint64_t full_bar[kStages], empty_bar[kStages];
-    __shared__ __align__(8) uint64_t accf_bar[2], acce_bar[2], drain_bar;
+    unsigned char *recring = ring + (size_t)S * G::STAGE;  // kRecSlots x 512 bytes
+    __shared__ __align__(8) uint64_t full_bar[S], empty_bar[S];
+    __shared__ __align__(8) uint64_t rfull_bar[kRecSlots], rempty_bar[kRecSlots];
+    __shared__ __align__(8) uint64_t pfull_bar[2], pempty_bar[2], drain_bar;
     __shared__ uint32_t s_tmem;
     __shared__ volatile uint32_t s_abort;
 
@@ -201,13 +251,17 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
     const uint32_t units = a.n_obj * a.n_tiles;
 
     if (tid == 0) {
-        for (int s = 0; s < kStages; ++s) {
+        for (int s = 0; s < S; ++s) {
             mbar_init(&full_bar[s], kProducerThreads);
             mbar_init(&empty_bar[s], 1);
         }
+        for (int r = 0; r < kRecSlots; ++r) {
+            mbar_init(&rfull_bar[r], 1);
+            mbar_init(&rempty_bar[r], kProducerThreads);
+        }
         for (int b = 0; b < 2; ++b) {
-            mbar_init(&accf_bar[b], 1);
-            mbar_init(&acce_bar[b], kEpilogueThreads);
+            mbar_init(&pfull_bar[b], 1);
+            mbar_init(&pempty_bar[b], kEpilogueThreads);
         }
         mbar_init(&drain_bar, 1);
         s_abort = 0u;
@@ -225,88 +279,118 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
     tc_fence_after();
     const uint32_t tmem = s_tmem;
 
-    if (warp >= 5) {
+    if (warp >= kProducerWarp0) {
         // ---------------- producers ----------------
-        const uint32_t pt = (uint32_t)tid - 160u;
-        const uint32_t p = pt >> 1, h = pt & 1u;  // A: row p, observations 4h..4h+3
-        // B: std: m = pt / 4, observations 2(pt % 4) + {0, 1}; gen: m = pt / 8, obs pt % 8
-        const uint32_t bm = GEN ? (pt >> 3) : (pt >> 2);
-        const uint32_t bj0 = GEN ? (pt & 7u) : 2u * (pt & 3u);
-        constexpr int BJ = GEN ? 1 : 2;
+        const uint32_t pw = (uint32_t)(warp - kProducerWarp0);  // 0..7
+        // A: rows p and p + kTensorRowStep (the second by the record's rotation), the
+        // four observations 8h + 4qd .. of the K-block. One 8-byte store per row and
+        // matrix; a half-warp writes 8 rows x 16 bytes = 128 contiguous bytes.
+        const uint32_t qd = (lane >> 3) & 1u, h = lane >> 4;
+        const uint32_t p = 16u * pw + (lane & 7u);
+        const uint32_t ja = 8u * h + 4u * qd;
+        const uint32_t offa0 = kmaj_off(p, ja), offa1 = kmaj_off(p + kTensorRowStep, ja);
+        // Z: row m, observations zj, zj+1 of K half zh; a warp writes 8 rows x 16 bytes
+        const bool zact = GEN ? pw < 4 : true;
+        const uint32_t zm = 8u * (pw >> 1) + (lane >> 2);
+        const uint32_t zh = pw & 1u;
+        const uint32_t zj = 8u * zh + 2u * (lane & 3u);
         uint32_t g = 0;
         for (uint32_t u = blockIdx.x; u < units && !s_abort; u += gridDim.x) {
             const UnitInfo w = unit_info(a, u);
             const uint32_t kT = w.tile * (uint32_t)G::TILE;
-            const uint32_t nkb = (w.n + kTK - 1) / kTK;
-            const ObsRec *rec = static_cast<const ObsRec *>(a.rec) + w.row0;
-            for (uint32_t kb = 0; kb < nkb; ++kb, ++g) {
-                const uint32_t s = g % kStages, use = g / kStages;
-                if (!mbar_wait(&empty_bar[s], (use & 1u) ^ 1u, &s_abort, a.status)) break;
+            const ObjInfo &ob = a.objs[w.o];
+            const float sc0 = ob.tsc0, sc1 = ob.tsc1;
+            for (uint32_t kb = 0; kb < w.nkb; ++kb, ++g) {
+                const uint32_t r = g % kRecSlots, ur = g / kRecSlots;
+                const uint32_t s = g % S, us = g / S;
+                if (!mbar_wait(&rfull_bar[r], ur & 1u, &s_abort, a.status)) break;
+                const unsigned char *rs = recring + (size_t)r * kRecSlotBytes;
+                const uint32_t cnt = min((uint32_t)kTK, w.n - kb * kTK);
+                uint4 ra[4];
+                float4 va[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const uint32_t jj = min(ja + (uint32_t)q, cnt - 1u);
+                    ra[q] = *reinterpret_cast<const uint4 *>(rs + 32u * jj);
+                    va[q] = *reinterpret_cast<const float4 *>(rs + 32u * jj + 16u);
+                }
+                uint2 rb[2];
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    const uint32_t jj = min(zj + (uint32_t)q, cnt - 1u);
+                    rb[q] = *reinterpret_cast<const uint2 *>(rs + 32u * jj + 8u);
+                }
+                // the slot's next bulk copy is an async-proxy write: order these
+                // generic-proxy reads before it (write-after-read across proxies)
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_arrive(&rempty_bar[r]);
+                if (!mbar_wait(&empty_bar[s], (us & 1u) ^ 1u, &s_abort, a.status)) break;
                 unsigned char *st = ring + (size_t)s * G::STAGE;
-                // A operands: row p, four observations
+                // ---- A operands ----
                 {
-                    float ar[4], ai[4], a3r[4], a3i[4], a2r[4], a2i[4];
                     const uint32_t ka = kT + p;
+                    // values [row][quantity][observation]
+                    float x0[2][4], x1[2][4], x2[2][4], x3[2][4], x4[2][4], x5[2][4];
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
-                        const uint32_t j = kb * kTK + 4u * h + (uint32_t)q;
-                        const bool valid = j < w.n;
-                        const uint4 r0 = __ldg(reinterpret_cast<const uint4 *>(rec + (valid ? j : w.n - 1)));
-                        const float4 r1 =
-                            __ldg(reinterpret_cast<const float4 *>(rec + (valid ? j : w.n - 1)) + 1);
-                        const uint64_t ph = (uint64_t)ka * r0.z + (((uint64_t)r0.y << 32) | r0.x);
-                        const uint32_t hi = (uint32_t)(ph >> 32) + ka * r0.w;
-                        float sn, cs;
-                        turn_sincos(hi, sn, cs);
-                        const float v0 = valid ? r1.x : 0.0f;
-                        ar[q] = v0 * cs;
-                        ai[q] = v0 * sn;
-                        if (GEN) {
-                            const float v1 = valid ? r1.y : 0.0f;
-                            a3r[q] = v1 * cs;
-                            a3i[q] = v1 * sn;
-                            // weighted doubled angle: w cos 2t, w sin 2t
-                            a2r[q] = v0 * fmaf(cs, cs, -sn * sn);
-                            a2i[q] = v0 * (2.0f * cs * sn);
-                        } else {
-                            a2r[q] = valid ? fmaf(cs, cs, -sn * sn) : 0.0f;
-                            a2i[q] = valid ? 2.0f * cs * sn : 0.0f;
+                        const bool valid = ja + (uint32_t)q < cnt;
+                        const uint64_t ph =
+                            (uint64_t)ka * ra[q].z + (((uint64_t)ra[q].y << 32) | ra[q].x);
+                        const uint32_t hi = (uint32_t)(ph >> 32) + ka * ra[q].w;
+                        float sn[2], cs[2];
+                        turn_sincos(hi, sn[0], cs[0]);
+                        cs[1] = fmaf(cs[0], va[q].z, -sn[0] * va[q].w);  // rotate by s grid points
+                        sn[1] = fmaf(sn[0], va[q].z, cs[0] * va[q].w);
+                        const float v0 = valid ? va[q].x * sc0 : 0.0f;
+                        const float v1 = valid ? va[q].y * sc1 : 0.0f;
+#pragma unroll
+                        for (int rr = 0; rr < 2; ++rr) {
+                            const float c2 = fmaf(cs[rr], cs[rr], -sn[rr] * sn[rr]);
+                            const float s2 = 2.0f * cs[rr] * sn[rr];
+                            x0[rr][q] = v0 * cs[rr];
+                            x1[rr][q] = v0 * sn[rr];
+                            if (GEN) {
+                                x2[rr][q] = v1 * cs[rr];
+                                x3[rr][q] = v1 * sn[rr];
+                                x4[rr][q] = v0 * c2;  // weighted doubled angle
+                                x5[rr][q] = v0 * s2;
+                            } else {
+                                x2[rr][q] = valid ? c2 : 0.0f;
+                                x3[rr][q] = valid ? s2 : 0.0f;
+                            }
                         }
                     }
-                    const uint32_t off = kmaj_off(p, 4u * h);
-                    auto put4 = [&](int mat, const float (&x)[4]) {
-                        uint32_t hi[4], lo[4];
+                    auto put4 = [&](int mat, int rr, const float (&x)[2][4]) {
+                        float hi[4], lo[4];
 #pragma unroll
-                        for (int q = 0; q < 4; ++q) split_tf32(x[q], hi[q], lo[q]);
-                        unsigned char *base = st + G::A_OFF + (size_t)mat * G::A_BYTES + off;
-                        *reinterpret_cast<uint4 *>(base) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-                        *reinterpret_cast<uint4 *>(base + G::A_BYTES) =
-                            make_uint4(lo[0], lo[1], lo[2], lo[3]);
+                        for (int q = 0; q < 4; ++q) vsplit(x[rr][q], hi[q], lo[q]);
+                        unsigned char *base = st + (size_t)mat * G::A_BYTES + (rr ? offa1 : offa0);
+                        *reinterpret_cast<uint2 *>(base) =
+                            make_uint2(pack_h2(hi[0], hi[1]), pack_h2(hi[2], hi[3]));
+                        *reinterpret_cast<uint2 *>(base + G::A_BYTES) =
+                            make_uint2(pack_h2(lo[0], lo[1]), pack_h2(lo[2], lo[3]));
                     };
-                    // matrix order: group g: (re hi, re lo, im hi, im lo) at 4g..4g+3
-                    put4(0, ar);
-                    put4(2, ai);
-                    if (GEN) {
-                        put4(4, a3r);
-                        put4(6, a3i);
-                        put4(8, a2r);
-                        put4(10, a2i);
-                    } else {
-                        put4(4, a2r);
-                        put4(6, a2i);
+                    // matrix order: group g at 4g: re hi, re lo, im hi, im lo
+#pragma unroll
+                    for (int rr = 0; rr < 2; ++rr) {
+                        put4(0, rr, x0);
+                        put4(2, rr, x1);
+                        put4(4, rr, x2);
+                        put4(6, rr, x3);
+                        if (GEN) {
+                            put4(8, rr, x4);
+                            put4(10, rr, x5);
+                        }
                     }
                 }
-                // Z operands: Z = [-Bi; Br; Bi] for angle m beta and 2 m beta
-                {
-                    float cr[BJ], si[BJ], c2[BJ], s2[BJ];
-                    const uint32_t kb128 = 128u * bm;
+                // ---- Z operands: Z = [-Bi; Br; Bi] for the angles m beta and 2 m beta ----
+                if (zact) {
+                    float cr[2], si[2], c2[2], s2[2];
+                    const uint32_t kb128 = 128u * zm;
 #pragma unroll
-                    for (int q = 0; q < BJ; ++q) {
-                        const uint32_t j = kb * kTK + bj0 + (uint32_t)q;
-                        const uint4 r0 =
-                            __ldg(reinterpret_cast<const uint4 *>(rec + (j < w.n ? j : w.n - 1)));
-                        const uint64_t ph = (uint64_t)kb128 * r0.z;
-                        const uint32_t hi = (uint32_t)(ph >> 32) + kb128 * r0.w;
+                    for (int q = 0; q < 2; ++q) {
+                        const uint64_t ph = (uint64_t)kb128 * rb[q].x;
+                        const uint32_t hi = (uint32_t)(ph >> 32) + kb128 * rb[q].y;
                         float sn, cs;
                         turn_sincos(hi, sn, cs);
                         cr[q] = cs;
@@ -314,82 +398,109 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                         c2[q] = fmaf(cs, cs, -sn * sn);
                         s2[q] = 2.0f * cs * sn;
                     }
-                    auto putz = [&](int zmat, uint32_t row, const float *x, bool neg) {
+                    auto putz = [&](int zmat, uint32_t row, const float (&x)[2], bool neg) {
                         unsigned char *base =
-                            st + G::Z_OFF + (size_t)zmat * G::Z_BYTES + kmaj_off(row, bj0);
-                        uint32_t hi[BJ], lo[BJ];
-#pragma unroll
-                        for (int q = 0; q < BJ; ++q) split_tf32(neg ? -x[q] : x[q], hi[q], lo[q]);
-                        if (BJ == 2) {
-                            *reinterpret_cast<uint2 *>(base) = make_uint2(hi[0], hi[BJ - 1]);
-                            *reinterpret_cast<uint2 *>(base + G::Z_BYTES) = make_uint2(lo[0], lo[BJ - 1]);
-                        } else {
-                            *reinterpret_cast<uint32_t *>(base) = hi[0];
-                            *reinterpret_cast<uint32_t *>(base + G::Z_BYTES) = lo[0];
+                            st + G::Z_OFF + (size_t)zmat * G::Z_BYTES + kmaj_off(row, zj);
+                        float hi0, lo0, hi1, lo1;
+                        vsplit(x[0], hi0, lo0);
+                        vsplit(x[1], hi1, lo1);
+                        if (neg) {
+                            hi0 = -hi0;
+                            lo0 = -lo0;
+                            hi1 = -hi1;
+                            lo1 = -lo1;
                         }
+                        *reinterpret_cast<uint32_t *>(base) = pack_h2(hi0, hi1);
+                        *reinterpret_cast<uint32_t *>(base + G::Z_BYTES) = pack_h2(lo0, lo1);
                     };
                     constexpr uint32_t NM = G::NM;
                     // angle m beta: Z matrices 0 (hi), 1 (lo); 2 m beta: 2 (hi), 3 (lo)
-                    putz(0, bm, si, true);
-                    putz(0, NM + bm, cr, false);
-                    putz(0, 2 * NM + bm, si, false);
-                    putz(2, bm, s2, true);
-                    putz(2, NM + bm, c2, false);
-                    putz(2, 2 * NM + bm, s2, false);
+                    putz(0, zm, si, true);
+                    putz(0, NM + zm, cr, false);
+                    putz(0, 2 * NM + zm, si, false);
+                    putz(2, zm, s2, true);
+                    putz(2, NM + zm, c2, false);
+                    putz(2, 2 * NM + zm, s2, false);
                 }
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 mbar_arrive(&full_bar[s]);
             }
         }
+    } else if (warp == 5) {
+        // ---------------- record loader ----------------
+        if (lane == 0) {
+            const ObsRec *rec = static_cast<const ObsRec *>(a.rec);
+            uint32_t g = 0;
+            for (uint32_t u = blockIdx.x; u < units && !s_abort; u += gridDim.x) {
+                const UnitInfo w = unit_info(a, u);
+                for (uint32_t kb = 0; kb < w.nkb; ++kb, ++g) {
+                    const uint32_t r = g % kRecSlots, ur = g / kRecSlots;
+                    if (!mbar_wait(&rempty_bar[r], (ur & 1u) ^ 1u, &s_abort, a.status)) break;
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    const uint32_t cnt = min((uint32_t)kTK, w.n - kb * kTK);
+                    const uint32_t bytes = cnt * 32u;
+                    mbar_expect_tx(&rfull_bar[r], bytes);
+                    bulk_copy_g2s(recring + (size_t)r * kRecSlotBytes, rec + w.row0 + (uint64_t)kb * kTK,
+                                  bytes, &rfull_bar[r]);
+                }
+            }
+        }
+        __syncwarp();
     } else if (warp == 4) {
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
-            constexpr uint32_t idesc = idesc_tf32(kTP, G::N);
-            uint32_t g = 0, lu = 0;
+            constexpr uint32_t idesc = idesc_f16(kTP, G::N);
+            uint32_t g = 0, gp = 0;
             bool ok = true;
-            for (uint32_t u = blockIdx.x; u < units && ok; u += gridDim.x, ++lu) {
+            for (uint32_t u = blockIdx.x; u < units && ok; u += gridDim.x) {
                 const UnitInfo w = unit_info(a, u);
-                const uint32_t nkb = (w.n + kTK - 1) / kTK;
-                const uint32_t buf = lu & 1u, ub = lu >> 1;
-                if (!mbar_wait(&acce_bar[buf], (ub & 1u) ^ 1u, &s_abort, a.status)) break;
-                tc_fence_after();
-                const uint32_t d0 = tmem + buf * kBufCols;
-                for (uint32_t kb = 0; kb < nkb; ++kb, ++g) {
-                    const uint32_t s = g % kStages, use = g / kStages;
-                    if (!mbar_wait(&full_bar[s], use & 1u, &s_abort, a.status)) { ok = false; break; }
-                    tc_fence_after();
-                    const uint32_t sb = smem_u32(ring + (size_t)s * G::STAGE);
-                    auto adesc = [&](int mat) { return sdesc(sb + G::A_OFF + mat * G::A_BYTES); };
-                    // right factors: [Br; Bi] = Z rows NM.., [-Bi; Br] = Z rows 0..
-                    auto zdesc = [&](int zmat, int row0) {
-                        return sdesc(sb + G::Z_OFF + zmat * G::Z_BYTES + row0 * 32);
-                    };
-                    const uint32_t acc0 = kb > 0 ? 1u : 0u;
-                    // one complex product: D += A_g (re, im) x Z_z, split-TF32
-                    auto cplx = [&](uint32_t d, int ga, int zz) {
-                        const uint64_t arh = adesc(4 * ga + 0), arl = adesc(4 * ga + 1);
-                        const uint64_t aih = adesc(4 * ga + 2), ail = adesc(4 * ga + 3);
-                        const uint64_t bh = zdesc(zz, G::NM), bl = zdesc(zz + 1, G::NM);
-                        const uint64_t nh = zdesc(zz, 0), nl = zdesc(zz + 1, 0);
-                        mma_tf32(d, arh, bh, idesc, acc0);
-                        mma_tf32(d, arh, bl, idesc, 1u);
-                        mma_tf32(d, arl, bh, idesc, 1u);
-                        mma_tf32(d, aih, nh, idesc, 1u);
-                        mma_tf32(d, aih, nl, idesc, 1u);
-                        mma_tf32(d, ail, nh, idesc, 1u);
-                    };
-                    if (GEN) {
-                        cplx(d0 + 0, 0, 0);                    // [C | S]
-                        cplx(d0 + (uint32_t)G::N, 1, 0);       // [YC | YS]
-                        cplx(d0 + 2u * (uint32_t)G::N, 2, 2);  // [C2 | S2]
-                    } else {
-                        cplx(d0 + 0, 0, 0);                    // [XC | XS]
-                        cplx(d0 + (uint32_t)G::N, 1, 2);       // [C2 | S2]
+                for (uint32_t kb0 = 0; kb0 < w.nkb && ok; kb0 += kPassKB, ++gp) {
+                    const uint32_t buf = gp & 1u, ub = gp >> 1;
+                    if (!mbar_wait(&pempty_bar[buf], (ub & 1u) ^ 1u, &s_abort, a.status)) {
+                        ok = false;
+                        break;
                     }
-                    mma_commit(&empty_bar[s]);
+                    tc_fence_after();
+                    const uint32_t d0 = tmem + buf * kBufCols;
+                    const uint32_t kb1 = min(w.nkb, kb0 + (uint32_t)kPassKB);
+                    for (uint32_t kb = kb0; kb < kb1; ++kb, ++g) {
+                        const uint32_t s = g % S, use = g / S;
+                        if (!mbar_wait(&full_bar[s], use & 1u, &s_abort, a.status)) {
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint32_t sb = smem_u32(ring + (size_t)s * G::STAGE);
+                        const uint32_t acc0 = kb > kb0 ? 1u : 0u;
+                        // one complex product: D += A_g (re, im) x Z window, split FP16
+                        auto cplx = [&](uint32_t d, int ga, int zz) {
+                            const uint32_t ab = sb + (uint32_t)(4 * ga) * G::A_BYTES;
+                            const uint64_t arh = sdesc(ab), arl = sdesc(ab + G::A_BYTES);
+                            const uint64_t aih = sdesc(ab + 2 * G::A_BYTES);
+                            const uint64_t ail = sdesc(ab + 3 * G::A_BYTES);
+                            const uint32_t zb = sb + G::Z_OFF + (uint32_t)zz * G::Z_BYTES;
+                            // [Br; Bi] = Z rows NM.., [-Bi; Br] = Z rows 0..
+                            const uint64_t bh = sdesc(zb + G::NM * 32), bl = sdesc(zb + G::Z_BYTES + G::NM * 32);
+                            const uint64_t nh = sdesc(zb), nl = sdesc(zb + G::Z_BYTES);
+                            mma_f16(d, arh, bh, idesc, acc0);
+                            mma_f16(d, arh, bl, idesc, 1u);
+                            mma_f16(d, arl, bh, idesc, 1u);
+                            mma_f16(d, aih, nh, idesc, 1u);
+                            mma_f16(d, aih, nl, idesc, 1u);
+                            mma_f16(d, ail, nh, idesc, 1u);
+                        };
+                        if (GEN) {
+                            cplx(d0 + 0, 0, 0);                    // [C | S]
+                            cplx(d0 + (uint32_t)G::N, 1, 0);       // [YC | YS]
+                            cplx(d0 + 2u * (uint32_t)G::N, 2, 2);  // [C2 | S2]
+                        } else {
+                            cplx(d0 + 0, 0, 0);                    // [XC | XS]
+                            cplx(d0 + (uint32_t)G::N, 1, 2);       // [C2 | S2]
+                        }
+                        mma_commit(&empty_bar[s]);
+                    }
+                    if (ok) mma_commit(&pfull_bar[buf]);
                 }
-                if (!ok) break;
-                mma_commit(&accf_bar[buf]);
             }
             // every issued MMA has completed before TMEM is released
             mma_commit(&drain_bar);
@@ -399,72 +510,104 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
         }
         __syncwarp();
     } else {
-        // ---------------- epilogue (warps 0-3: TMEM lanes 32 warp ..) ----------------
+        // ---------------- fold and epilogue (warps 0-3: TMEM lanes 32 warp ..) ----------------
         const uint32_t pl = (uint32_t)warp * 32u + (uint32_t)lane;
         const uint32_t lane_base = ((uint32_t)warp * 32u) << 16;
-        uint32_t lu = 0;
-        for (uint32_t u = blockIdx.x; u < units; u += gridDim.x, ++lu) {
+        const uint32_t run = tmem + lane_base + kRunCol;
+        uint32_t gp = 0;
+        bool ok = true;
+        for (uint32_t u = blockIdx.x; u < units && ok; u += gridDim.x) {
             const UnitInfo w = unit_info(a, u);
-            const uint32_t buf = lu & 1u, ub = lu >> 1;
-            if (!mbar_wait(&accf_bar[buf], ub & 1u, &s_abort, a.status)) break;
-            tc_fence_after();
-            const uint32_t d0 = tmem + lane_base + buf * kBufCols;
-            const uint32_t kT = w.tile * (uint32_t)G::TILE;
-            const ObjInfo &ob = a.objs[w.o];
-            const float nrm = ob.norm32;
-            const uint64_t out0 = (uint64_t)w.o * a.n_freq;
-            float bp = 0.0f;
-            uint32_t bk = 0xffffffffu;
-            if (w.tile == 0 && pl == 0) bk = 0;  // the reference's (power 0, index 0) start
+            const uint32_t npass = (w.nkb + kPassKB - 1) / kPassKB;
+            for (uint32_t pi = 0; pi < npass; ++pi, ++gp) {
+                const uint32_t buf = gp & 1u, ub = gp >> 1;
+                if (!mbar_wait(&pfull_bar[buf], ub & 1u, &s_abort, a.status)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t part = tmem + lane_base + buf * kBufCols;
+                if (pi + 1 < npass) {
+                    // fold: running = (pi ? running : 0) + partial
 #pragma unroll 1
-            for (int m0 = 0; m0 < G::NM; m0 += 16) {
-                float re[16], im[16], r2[16], i2[16];
-                float yr[16], yi[16];
-                tmem_ld16(d0 + (uint32_t)m0, re);
-                tmem_ld16(d0 + (uint32_t)(G::NM + m0), im);
-                if (GEN) {
-                    tmem_ld16(d0 + (uint32_t)(G::N + m0), yr);
-                    tmem_ld16(d0 + (uint32_t)(G::N + G::NM + m0), yi);
-                    tmem_ld16(d0 + (uint32_t)(2 * G::N + m0), r2);
-                    tmem_ld16(d0 + (uint32_t)(2 * G::N + G::NM + m0), i2);
-                } else {
-                    tmem_ld16(d0 + (uint32_t)(G::N + m0), r2);
-                    tmem_ld16(d0 + (uint32_t)(G::N + G::NM + m0), i2);
-                }
-                tmem_wait_ld();
+                    for (uint32_t c = 0; c < (uint32_t)G::W; c += 8) {
+                        uint32_t x[8], y[8];
+                        tmem_ld8(part + c, x);
+                        if (pi) tmem_ld8(run + c, y);
+                        tmem_wait_ld();
+                        float v[8];
 #pragma unroll
-                for (int i = 0; i < 16; ++i) {
-                    const uint32_t k = kT + pl + (uint32_t)kTP * (uint32_t)(m0 + i);
-                    float P;
-                    if (GEN) {
-                        // CC = (W + sum w cos 2t) / 2, CS = sum w sin 2t / 2, W = wsum_f
-                        const float W = __fdividef(1.0f, ob.invw32);
-                        P = gen_power_f(ob.invw32, ob.ybar32, re[i], im[i], yr[i], yi[i],
-                                        0.5f * (W + r2[i]), 0.5f * i2[i]) *
-                            nrm;
-                    } else {
-                        const float N = (float)w.n;
-                        P = std_power_f(N, re[i], im[i], 0.5f * (N + r2[i]), 0.5f * i2[i]) * nrm;
+                        for (int i = 0; i < 8; ++i)
+                            v[i] = __uint_as_float(x[i]) + (pi ? __uint_as_float(y[i]) : 0.0f);
+                        tmem_st8(run + c, v);
                     }
-                    if (k < a.n_freq) {
-                        if (a.pgram) store_out<OutT>(a.pgram, out0 + k, P);
-                        if (better(P, k, bp, bk)) { bp = P; bk = k; }
-                    }
+                    tmem_wait_st();
+                    tc_fence_before();
+                    mbar_arrive(&pempty_bar[buf]);
+                    continue;
                 }
-            }
-            tc_fence_before();
-            mbar_arrive(&acce_bar[buf]);
-            if (a.best_key) {
+                // last pass: running + partial -> power
+                const uint32_t kT = w.tile * (uint32_t)G::TILE;
+                const ObjInfo &ob = a.objs[w.o];
+                const float nrm = ob.norm32;
+                const float us0 = 1.0f / ob.tsc0, us1 = 1.0f / ob.tsc1;  // powers of two
+                const uint64_t out0 = (uint64_t)w.o * a.n_freq;
+                float bp = 0.0f;
+                uint32_t bk = 0xffffffffu;
+                if (w.tile == 0 && pl == 0) bk = 0;  // the reference's (power 0, index 0) start
+                constexpr int NQ = 2 * G::NAG;       // quantities per frequency
+#pragma unroll 1
+                for (int m0 = 0; m0 < G::NM; m0 += 8) {
+                    float q[NQ][8];
 #pragma unroll
-                for (int off = 16; off > 0; off >>= 1) {
-                    const float op = __shfl_xor_sync(0xffffffffu, bp, off);
-                    const uint32_t ok = __shfl_xor_sync(0xffffffffu, bk, off);
-                    if (better(op, ok, bp, bk)) { bp = op; bk = ok; }
+                    for (int k = 0; k < NQ; ++k) {
+                        // quantity k: group k/2, real (even k) or imaginary part
+                        const uint32_t col = (uint32_t)((k >> 1) * G::N + (k & 1) * G::NM + m0);
+                        uint32_t x[8], y[8];
+                        tmem_ld8(part + col, x);
+                        if (npass > 1) tmem_ld8(run + col, y);
+                        tmem_wait_ld();
+#pragma unroll
+                        for (int i = 0; i < 8; ++i)
+                            q[k][i] = __uint_as_float(x[i]) + (npass > 1 ? __uint_as_float(y[i]) : 0.0f);
+                    }
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        const uint32_t k = kT + pl + (uint32_t)kTP * (uint32_t)(m0 + i);
+                        float P;
+                        if (GEN) {
+                            // CC = (W + sum w cos 2t) / 2, CS = sum w sin 2t / 2, W = wsum_f
+                            const float Wt = __fdividef(1.0f, ob.invw32);
+                            P = gen_power_f(ob.invw32, ob.ybar32, q[0][i] * us0, q[1][i] * us0,
+                                            q[2][i] * us1, q[3][i] * us1,
+                                            0.5f * fmaf(q[4][i], us0, Wt), 0.5f * q[5][i] * us0) *
+                                nrm;
+                        } else {
+                            const float N = (float)w.n;
+                            P = std_power_f(N, q[0][i] * us0, q[1][i] * us0, 0.5f * (N + q[2][i]),
+                                            0.5f * q[3][i]) *
+                                nrm;
+                        }
+                        if (k < a.n_freq) {
+                            if (a.pgram) store_out<OutT>(a.pgram, out0 + k, P);
+                            if (better(P, k, bp, bk)) { bp = P; bk = k; }
+                        }
+                    }
                 }
-                if (lane == 0 && bp > 0.0f)
-                    atomicMax(a.best_key + w.o,
-                              ((unsigned long long)__float_as_uint(bp) << 32) |
-                                  (unsigned long long)(~bk));
+                tc_fence_before();
+                mbar_arrive(&pempty_bar[buf]);
+                if (a.best_key) {
+#pragma unroll
+                    for (int off = 16; off > 0; off >>= 1) {
+                        const float op = __shfl_xor_sync(0xffffffffu, bp, off);
+                        const uint32_t ok2 = __shfl_xor_sync(0xffffffffu, bk, off);
+                        if (better(op, ok2, bp, bk)) { bp = op; bk = ok2; }
+                    }
+                    if (lane == 0 && bp > 0.0f)
+                        atomicMax(a.best_key + w.o,
+                                  ((unsigned long long)__float_as_uint(bp) << 32) |
+                                      (unsigned long long)(~bk));
+                }
             }
         }
     }
@@ -481,7 +624,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
 
 template <bool GEN>
 size_t tensor_smem() {
-    return (size_t)kStages * TGeo<GEN>::STAGE + 1024;
+    return (size_t)TGeo<GEN>::STAGES * TGeo<GEN>::STAGE + (size_t)kRecSlots * kRecSlotBytes + 1024;
 }
 
 template <bool GEN, typename OutT>
@@ -503,7 +646,8 @@ uint32_t tensor_tile_freqs(int variant) {
 size_t tensor_smem_bytes(int variant) { return variant ? tensor_smem<true>() : tensor_smem<false>(); }
 
 cudaError_t launch_tensor(int variant, int dtype, const MixedArgs &a, int grid, cudaStream_t st) {
-    if (variant == 0) return dtype == 0 ? launch_t<false, float>(a, grid, st) : launch_t<false, double>(a, grid, st);
+    if (variant == 0)
+        return dtype == 0 ? launch_t<false, float>(a, grid, st) : launch_t<false, double>(a, grid, st);
     return dtype == 0 ? launch_t<true, float>(a, grid, st) : launch_t<true, double>(a, grid, st);
 }
 
