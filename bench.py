@@ -5,8 +5,9 @@ Workload (the reference's headline batch): 999 objects with log-normal observati
 counts (round(LogNormal(ln 150, 0.6)) clipped to [20, 1500], ~176k rows, seeded,
 synthetic), standard L-S, 1e6 angular frequencies in [1.005, 150.796). One step =
 one batch periodogram with the fused per-object argmax, mixed precision form, inputs
-resident in HBM, replayed from a CUDA-graph plan (lsgb_plan_launch). Metric:
-observation x frequency pairs per second.
+resident in HBM, replayed from a CUDA-graph plan (lsgb_plan_launch), in the engine's
+default form (the tensor-core form: split-FP16 tcgen05 MMAs, FP32 accumulation and folds,
+FP64 phase anchors). Metric: observation x frequency pairs per second.
 
 Also reported on the same line:
   plain_fp64   the FP64 drop-in form on the first frequencies of the same grid;
@@ -14,8 +15,12 @@ Also reported on the same line:
                inputs in, best index/power out, copies inside the timed region;
   e2e_dropin   LombScarglePy of libpylsnoerrorfloat.so (MODE 1) returning the full
                periodogram to a host buffer, as source/lombscarglegpu.py calls it;
-  roofline     the mixed kernel's FP32-pipe ops (8 per pair) per second against the
-               FP32 FMA peak measured in the same run (cuBLAS SGEMM, TF32 off);
+  roofline     the tensor kernel's FP16 MMA flops (48 per pair, standard variant) per
+               second against the measured dense bf16/FP16 tensor peak
+               (MEASURED_PEAKS.json, burst);
+  cuda_core_form  the same batch in the CUDA-core mixed form (FP32 second-order recurrence),
+               with its FP32-pipe ops per pair against the FP32 FMA peak measured in the
+               same run (cuBLAS SGEMM, TF32 off);
   cpu_baseline the FP64 oracle (the reference's CPU algorithm) on all host cores;
   clocks       nvidia-smi samples taken during the timed region;
   serving      the continuous-batching loop on a Poisson stream (100,000 objects at
@@ -39,9 +44,24 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-METRIC = "obs x freq pairs/s (mixed FP32-recurrence form, 1 GB300)"
+METRIC = "obs x freq pairs/s (mixed form, 1 GB300)"
 UNIT = "pairs/s"
-OPS_PER_PAIR_STD = 8  # 4 rotation + 4 accumulation FP32-pipe ops per (obs, freq) pair
+# tensor form, standard variant: two complex products (v e^ia x e^imb, e^2ia x e^2imb),
+# each 4 real MACs x 3 split-FP16 products = 24 MACs = 48 flops per (obs, freq) pair
+TENSOR_FLOPS_PER_PAIR_STD = 48
+# CUDA-core form 2 (F = 12): per observation and thread 4 (odd-lane offset) + 8 (rotation
+# to the second pair) + 4 x 4 (second-order steps) + 6 x 8 (accumulations) = 76 FP32-pipe
+# lane-ops for 12 pairs
+CUDA_CORE_SHAPE_STD = (12, 256, 2, 2, 0)
+OPS_PER_PAIR_CUDA_CORE = 76 / 12
+# DRAM read + write bytes of one tensor-kernel launch, from the ncu capture of the same
+# batch at 1e5 frequencies (profiles/tensor_kernel_std_999obj_1e5freq.md): the ObsRec
+# records and per-object tables are read from DRAM once per launch whatever the grid
+# size (re-reads across frequency tiles hit L2), and nothing is written without a
+# periodogram
+TENSOR_DRAM_BYTES_PER_LAUNCH = 5.78e6
+MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
+FALLBACK_BF16_TFLOPS = 1900.0
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -103,6 +123,16 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def tensor_peak_tflops():
+    """(peak TFLOP/s, source) of dense bf16/FP16 MMA: the measured burst figure,
+    else the fallback."""
+    try:
+        d = json.loads(MEASURED_PEAKS.read_text())
+        return float(d["bf16_tflops"]), "MEASURED_PEAKS.json bf16_tflops (burst), of measured"
+    except (OSError, ValueError, KeyError):
+        return FALLBACK_BF16_TFLOPS, "fallback 1.9 PFLOP/s bf16 burst, of fallback"
 
 
 def fp32_peak_ops(torch, dev):
@@ -289,18 +319,45 @@ def main():
         return
     clocks = clk.summary()
     kms = float(np.mean(kern_ms))
-    ops = w.pairs * OPS_PER_PAIR_STD
-    peak_ops = fp32_peak_ops(torch, dev)
-    sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    achieved = ops / (kms / 1e3)
-    roofline = {"bound": "fp32", "achieved": achieved / 1e12, "peak": peak_ops / 1e12,
-                "unit": "Tops/s (FP32 pipe ops)", "frac": achieved / peak_ops, "traffic": None,
-                "peak_source": "cuBLAS SGEMM 8192^3, TF32 off, measured in this run (FMA ops/s)",
-                "ops_per_pair": OPS_PER_PAIR_STD, "kernel_ms": kms,
-                "frac_of_nominal_at_sampled_clock": (
-                    achieved / (128 * sms * clocks["sm_mhz"] * 1e6) if clocks["sm_mhz"] else None)}
-
+    shape = eng.get_tuning(0)  # (F, threads, min CTAs, form, unroll)
+    tensor_form = shape[3] == 3
     extra = {}
+    peak_ops = fp32_peak_ops(torch, dev)
+    if tensor_form:
+        peak_tf, peak_src = tensor_peak_tflops()
+        achieved = w.pairs * TENSOR_FLOPS_PER_PAIR_STD / (kms / 1e3) / 1e12
+        roofline = {"bound": "tensor", "achieved": achieved, "peak": peak_tf, "unit": "TFLOP/s",
+                    "frac": achieved / peak_tf, "traffic": TENSOR_DRAM_BYTES_PER_LAUNCH,
+                    "peak_source": peak_src, "flops_per_pair": TENSOR_FLOPS_PER_PAIR_STD,
+                    "kernel_ms": kms, "kernel": "tensor_kernel<standard> (lsgb_tensor.cu)"}
+        # the CUDA-core form on the same batch, against the FP32 FMA peak
+        saved = eng.get_tuning(0)
+        eng.set_tuning(0, *CUDA_CORE_SHAPE_STD)
+        try:
+            cm = []
+            for _ in range(3):
+                flush.zero_()
+                eng.run_device(0, "mixed", t, y, None, w.offsets, w.fmin, w.df, w.n_freq, True,
+                               None, bi, bp, stream)
+                cm.append(eng.last_kernel_ms())
+        finally:
+            eng.set_tuning(0, *saved)
+        cms = float(np.median(cm[1:]))
+        cach = w.pairs * OPS_PER_PAIR_CUDA_CORE / (cms / 1e3)
+        extra["cuda_core_form"] = {
+            "value": w.pairs / (cms / 1e3), "unit": UNIT, "kernel_ms": cms,
+            "shape": list(CUDA_CORE_SHAPE_STD),
+            "roofline": {"bound": "fp32", "achieved": cach / 1e12, "peak": peak_ops / 1e12,
+                         "unit": "Tops/s (FP32 pipe ops)", "frac": cach / peak_ops,
+                         "ops_per_pair": OPS_PER_PAIR_CUDA_CORE,
+                         "peak_source": "cuBLAS SGEMM 8192^3, TF32 off, measured in this run"}}
+    else:
+        achieved = w.pairs * OPS_PER_PAIR_CUDA_CORE / (kms / 1e3)
+        roofline = {"bound": "fp32", "achieved": achieved / 1e12, "peak": peak_ops / 1e12,
+                    "unit": "Tops/s (FP32 pipe ops)", "frac": achieved / peak_ops, "traffic": None,
+                    "peak_source": "cuBLAS SGEMM 8192^3, TF32 off, measured in this run",
+                    "ops_per_pair": OPS_PER_PAIR_CUDA_CORE, "kernel_ms": kms}
+
     # plain FP64 drop-in form on the first plain_freqs frequencies
     if args.plain_freqs:
         wp = w.subset_freqs(args.plain_freqs)
@@ -357,17 +414,18 @@ def main():
         sys.stdout.flush()
         os.dup2(devnull, 1)
         try:
-            for i in range(3):
+            for i in range(5):
                 t0 = time.perf_counter()
                 lib.LombScarglePy(ids, t32, y32, ones, w.n_rows, w.fmin, w.fmax, w.n_freq, 1, pg)
-                if i:
+                if i:  # the first call loads the library's kernels and sizes its buffers
                     dt.append(time.perf_counter() - t0)
         finally:
             sys.stdout.flush()
             os.dup2(saved, 1)
             os.close(saved)
             os.close(devnull)
-        extra["e2e_dropin"] = {"value": w.pairs / float(np.mean(dt)), "unit": UNIT,
+        extra["e2e_dropin"] = {"value": w.pairs / float(np.median(dt)), "unit": UNIT,
+                               "ms_per_call": [round(1e3 * x, 2) for x in dt],
                                "h2d_bytes_per_step": int(t32.nbytes * 3 + ids.nbytes),
                                "d2h_bytes_per_step": int(pg.nbytes),
                                "api": "LombScarglePy, libpylsnoerrorfloat.so, MODE 1, full pgram"}
@@ -389,11 +447,14 @@ def main():
     cpu = cpu_baseline(w, args.cpu_freqs) if args.cpu_freqs else None
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 (FP64 phase anchors)",
+            "vs_baseline": None,
+            "dtype": ("f32 via split-f16 tensor MMAs (FP64 phase anchors)" if tensor_form
+                      else "f32 (FP64 phase anchors)"),
             "data": "synthetic (seeded log-normal batch, stands in for the reference's missing "
                     "999-object file)",
             "config": {"workload": "lognormal_999obj_1e6freq_standard", "n_obj": w.n_obj,
-                       "rows": w.n_rows, "n_freq": w.n_freq, "form": "mixed", "seed": w.seed,
+                       "rows": w.n_rows, "n_freq": w.n_freq, "seed": w.seed,
+                       "form": "mixed, tensor-core" if tensor_form else "mixed, CUDA-core",
                        "l2": "flushed between timed steps (256 MiB write)",
                        "fmin": w.fmin, "fmax": w.fmax},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,

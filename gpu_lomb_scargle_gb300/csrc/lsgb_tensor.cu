@@ -24,7 +24,8 @@
 // a long accumulation grow linearly with its length. So a unit's observations are summed
 // in passes of kPassKB K-blocks into one of two TMEM partial buffers, and the epilogue
 // warps fold each finished pass into an FP32 running sum in TMEM with round-to-nearest
-// adds; the last pass of a unit is folded straight into the power computation.
+// adds, releasing the partial buffer at once; after the last pass of a unit they compute
+// the powers from the running sums.
 //
 // One persistent CTA per SM, warp-specialized:
 //   warps 0-3   fold and epilogue: TMEM lanes 32w.. (the lanes warp w may access), power
@@ -203,6 +204,30 @@ __device__ __forceinline__ void tmem_st8(uint32_t taddr, const float (&v)[8]) {
         "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
         "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
         "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
+        : "memory");
+}
+// 32 consecutive accumulator columns (asynchronous until tmem_wait_ld).
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+        "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+          "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+          "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+          "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&v)[32]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+        "%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(
+            taddr),
+        "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]),
+        "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]),
+        "r"(v[15]), "r"(v[16]), "r"(v[17]), "r"(v[18]), "r"(v[19]), "r"(v[20]), "r"(v[21]),
+        "r"(v[22]), "r"(v[23]), "r"(v[24]), "r"(v[25]), "r"(v[26]), "r"(v[27]), "r"(v[28]),
+        "r"(v[29]), "r"(v[30]), "r"(v[31])
         : "memory");
 }
 __device__ __forceinline__ void tmem_wait_ld() {
@@ -527,30 +552,33 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                 }
                 tc_fence_after();
                 const uint32_t part = tmem + lane_base + buf * kBufCols;
-                if (pi + 1 < npass) {
-                    // fold: running = (pi ? running : 0) + partial
+                // fold: running = (pi ? running : 0) + partial, 32 columns per round; the
+                // partial buffer is released as soon as it has been read
+                static_assert(G::W % 32 == 0, "fold in 32-column rounds");
 #pragma unroll 1
-                    for (uint32_t c = 0; c < (uint32_t)G::W; c += 8) {
-                        uint32_t x[8], y[8];
-                        tmem_ld8(part + c, x);
-                        if (pi) tmem_ld8(run + c, y);
-                        tmem_wait_ld();
-                        float v[8];
+                for (uint32_t c = 0; c < (uint32_t)G::W; c += 32) {
+                    uint32_t x[32], y[32];
+                    tmem_ld32(part + c, x);
+                    if (pi) tmem_ld32(run + c, y);
+                    tmem_wait_ld();
+                    if (pi) {
 #pragma unroll
-                        for (int i = 0; i < 8; ++i)
-                            v[i] = __uint_as_float(x[i]) + (pi ? __uint_as_float(y[i]) : 0.0f);
-                        tmem_st8(run + c, v);
+                        for (int i = 0; i < 32; ++i)
+                            x[i] = __float_as_uint(__uint_as_float(x[i]) + __uint_as_float(y[i]));
                     }
-                    tmem_wait_st();
-                    tc_fence_before();
-                    mbar_arrive(&pempty_bar[buf]);
-                    continue;
+                    tmem_st32(run + c, x);
                 }
-                // last pass: running + partial -> power
+                tmem_wait_st();
+                tc_fence_before();
+                mbar_arrive(&pempty_bar[buf]);
+                if (pi + 1 < npass) continue;
+                // last pass: power from the running sums
                 const uint32_t kT = w.tile * (uint32_t)G::TILE;
                 const ObjInfo &ob = a.objs[w.o];
                 const float nrm = ob.norm32;
                 const float us0 = 1.0f / ob.tsc0, us1 = 1.0f / ob.tsc1;  // powers of two
+                const float Wt = __fdividef(1.0f, ob.invw32);
+                const float Nf = (float)w.n;
                 const uint64_t out0 = (uint64_t)w.o * a.n_freq;
                 float bp = 0.0f;
                 uint32_t bk = 0xffffffffu;
@@ -558,33 +586,32 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                 constexpr int NQ = 2 * G::NAG;       // quantities per frequency
 #pragma unroll 1
                 for (int m0 = 0; m0 < G::NM; m0 += 8) {
-                    float q[NQ][8];
+                    // all loads of the chunk first, one wait
+                    uint32_t x[NQ][8];
 #pragma unroll
                     for (int k = 0; k < NQ; ++k) {
                         // quantity k: group k/2, real (even k) or imaginary part
                         const uint32_t col = (uint32_t)((k >> 1) * G::N + (k & 1) * G::NM + m0);
-                        uint32_t x[8], y[8];
-                        tmem_ld8(part + col, x);
-                        if (npass > 1) tmem_ld8(run + col, y);
-                        tmem_wait_ld();
-#pragma unroll
-                        for (int i = 0; i < 8; ++i)
-                            q[k][i] = __uint_as_float(x[i]) + (npass > 1 ? __uint_as_float(y[i]) : 0.0f);
+                        tmem_ld8(run + col, x[k]);
                     }
+                    tmem_wait_ld();
+                    float q[NQ][8];
+#pragma unroll
+                    for (int k = 0; k < NQ; ++k)
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) q[k][i] = __uint_as_float(x[k][i]);
 #pragma unroll
                     for (int i = 0; i < 8; ++i) {
                         const uint32_t k = kT + pl + (uint32_t)kTP * (uint32_t)(m0 + i);
                         float P;
                         if (GEN) {
                             // CC = (W + sum w cos 2t) / 2, CS = sum w sin 2t / 2, W = wsum_f
-                            const float Wt = __fdividef(1.0f, ob.invw32);
                             P = gen_power_f(ob.invw32, ob.ybar32, q[0][i] * us0, q[1][i] * us0,
                                             q[2][i] * us1, q[3][i] * us1,
                                             0.5f * fmaf(q[4][i], us0, Wt), 0.5f * q[5][i] * us0) *
                                 nrm;
                         } else {
-                            const float N = (float)w.n;
-                            P = std_power_f(N, q[0][i] * us0, q[1][i] * us0, 0.5f * (N + q[2][i]),
+                            P = std_power_f(Nf, q[0][i] * us0, q[1][i] * us0, 0.5f * (Nf + q[2][i]),
                                             0.5f * q[3][i]) *
                                 nrm;
                         }
@@ -594,8 +621,6 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                         }
                     }
                 }
-                tc_fence_before();
-                mbar_arrive(&pempty_bar[buf]);
                 if (a.best_key) {
 #pragma unroll
                     for (int off = 16; off > 0; off >>= 1) {
