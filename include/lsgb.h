@@ -44,7 +44,8 @@ extern "C" {
 
 /* precision form */
 #define LSGB_PLAIN_FP64 0 /* FP64 sincos for every pair, FP64 atan2 tau: the drop-in form */
-#define LSGB_MIXED 1      /* FP64 phase anchors + FP32 angle-addition recurrence */
+#define LSGB_MIXED 1      /* FP64 phase anchors + FP32-accurate sums: split-FP16 tensor-core
+                             products (default shape) or FP32 recurrences (CUDA-core shapes) */
 
 /* element type of t / y / dy / pgram / best_power */
 #define LSGB_F32 0
@@ -116,9 +117,11 @@ LSGB_API void lsgb_plan_destroy(lsgb_plan *plan);
  * (`packed`: 0 scalar rotation; 1 packed f32x2 rotation over consecutive frequencies;
  * 2 packed f32x2 over frequencies strided by the CTA width, advanced by the
  * second-order recurrence x[p+1] = 2 cos(phi) x[p] - x[p-1] where it is well
- * conditioned), and two observations per loop iteration (1) or one (0). 0 (-1 for the
- * last two) keeps the current value. Returns LSGB_ERR_INVALID for shapes that are not
- * compiled in. */
+ * conditioned; 3 the tensor-core form, with F = coarse steps per unit and 128 threads
+ * standing for its 128 fine steps: (32, 128, 1, 3, 0) standard and (16, 128, 1, 3, 0)
+ * generalized, the defaults), and two observations per loop iteration (1) or one (0).
+ * 0 (-1 for the last two) keeps the current value. Returns LSGB_ERR_INVALID for shapes
+ * that are not compiled in. */
 LSGB_API int lsgb_set_tuning(lsgb_engine *eng, int variant, int freqs_per_thread,
                              int threads_per_cta, int min_ctas_per_sm, int packed, int unroll);
 
@@ -190,7 +193,8 @@ LSGB_API int lsgb_mixed_shapes(int *out, int max_shapes);
  * over [-scale, scale]: *max_err receives the largest absolute difference. */
 LSGB_API int lsgb_fp64_sincos_check(lsgb_engine *eng, uint32_t n, double scale, double *max_err);
 
-/* Re-anchoring interval R of the mixed form's recurrence. 0 (default): every thread's
+/* Re-anchoring interval R of the CUDA-core mixed form's recurrence (R > 0 runs that
+ * form's consecutive-frequency rotation loop whatever the tuned shape). 0 (default): every thread's
  * run of F frequencies starts from an exact anchor, so no frequency is more than F-1
  * recurrence steps from one. R > 0: anchors only at multiples of R, each thread reaching
  * its run by up to R-1 extra FP32 steps -- the error of an R-step recurrence, at extra
