@@ -15,8 +15,8 @@
 // Each complex product is two real MMAs with N = 2 NM: [Re | Im] = Ar [Br | Bi]^T +
 // Ai [-Bi | Br]^T, the right factors being two overlapping row windows of
 // Z = [-Bi; Br; Bi]. FP32 accuracy on the FP16 tensor cores comes from the split
-// x = hi + lo (hi: x to 11 significant bits by Veltkamp's method, lo = x - hi rounded to
-// FP16), a b ~ ah bh + ah bl + al bh: every operand is a cosine or sine times a weight
+// x = hi + lo (hi: x rounded to 11 significant bits, lo = x - hi rounded to FP16),
+// a b ~ ah bh + ah bl + al bh: every operand is a cosine or sine times a weight
 // scaled into [-1, 1] by a power of two per object (ObjInfo::tsc0/tsc1), so hi + lo
 // carries x to about 2^-24 (lo may be subnormal, whose absolute spacing is 2^-24).
 //
@@ -105,12 +105,12 @@ __host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
     return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-// Veltkamp's split of an FP32 value (|x| <= 1) into hi with 11 significant bits (exact in
-// FP16 down to 2^-14) and lo = x - hi (exact in FP32; its FP16 rounding costs at most
-// 2^-25 absolute). Four FP32 operations, no conversions.
+// Split of an FP32 value (|x| <= 1) into hi with 11 significant bits (exact in FP16 down to
+// 2^-14) and lo = x - hi (exact in FP32; its FP16 rounding costs at most 2^-25 absolute):
+// hi is x rounded to nearest at the 11th significant bit, by an integer add and mask on its
+// bit pattern (a carry into the exponent gives the next power of two, still exact).
 __device__ __forceinline__ void vsplit(float x, float &hi, float &lo) {
-    const float t = __fmul_rn(x, 8193.0f);  // 2^13 + 1
-    hi = __fsub_rn(t, __fsub_rn(t, x));
+    hi = __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
     lo = __fsub_rn(x, hi);
 }
 
@@ -170,12 +170,22 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32
         : "memory");
 }
 
-__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
-                                        uint32_t accumulate) {
+// One complex product's six split-FP16 MMAs into d: a[0..3] = (re hi, re lo, im hi, im lo),
+// b[0..3] = (window [Br; Bi] hi, lo, window [-Bi; Br] hi, lo); the first MMA overwrites d
+// unless `accumulate`.
+__device__ __forceinline__ void mma_cplx6(uint32_t d, const uint64_t (&a)[4],
+                                          const uint64_t (&b)[4], uint32_t idesc,
+                                          uint32_t accumulate) {
     asm volatile(
-        "{ .reg .pred p; setp.ne.b32 p, %4, 0; "
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }" ::"r"(d_tmem),
-        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        "{ .reg .pred p0, pt; setp.ne.b32 p0, %9, 0; setp.eq.b32 pt, %9, %9;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %5, %10, p0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %6, %10, pt;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %2, %5, %10, pt;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %3, %7, %10, pt;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %3, %8, %10, pt;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %4, %7, %10, pt; }" ::"r"(d),
+        "l"(a[0]), "l"(a[1]), "l"(a[2]), "l"(a[3]), "l"(b[0]), "l"(b[1]), "l"(b[2]), "l"(b[3]),
+        "r"(accumulate), "r"(idesc)
         : "memory");
 }
 __device__ __forceinline__ void mma_commit(uint64_t *b) {
@@ -423,29 +433,30 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                         c2[q] = fmaf(cs, cs, -sn * sn);
                         s2[q] = 2.0f * cs * sn;
                     }
-                    auto putz = [&](int zmat, uint32_t row, const float (&x)[2], bool neg) {
+                    // each value split once; -x = (-hi) + (-lo) exactly
+                    float zh[4][2], zl[4][2];
+#pragma unroll
+                    for (int q = 0; q < 2; ++q) {
+                        vsplit(si[q], zh[0][q], zl[0][q]);
+                        vsplit(cr[q], zh[1][q], zl[1][q]);
+                        vsplit(s2[q], zh[2][q], zl[2][q]);
+                        vsplit(c2[q], zh[3][q], zl[3][q]);
+                    }
+                    auto putz = [&](int zmat, uint32_t row, int v, float sg) {
                         unsigned char *base =
                             st + G::Z_OFF + (size_t)zmat * G::Z_BYTES + kmaj_off(row, zj);
-                        float hi0, lo0, hi1, lo1;
-                        vsplit(x[0], hi0, lo0);
-                        vsplit(x[1], hi1, lo1);
-                        if (neg) {
-                            hi0 = -hi0;
-                            lo0 = -lo0;
-                            hi1 = -hi1;
-                            lo1 = -lo1;
-                        }
-                        *reinterpret_cast<uint32_t *>(base) = pack_h2(hi0, hi1);
-                        *reinterpret_cast<uint32_t *>(base + G::Z_BYTES) = pack_h2(lo0, lo1);
+                        *reinterpret_cast<uint32_t *>(base) = pack_h2(sg * zh[v][0], sg * zh[v][1]);
+                        *reinterpret_cast<uint32_t *>(base + G::Z_BYTES) =
+                            pack_h2(sg * zl[v][0], sg * zl[v][1]);
                     };
                     constexpr uint32_t NM = G::NM;
                     // angle m beta: Z matrices 0 (hi), 1 (lo); 2 m beta: 2 (hi), 3 (lo)
-                    putz(0, zm, si, true);
-                    putz(0, NM + zm, cr, false);
-                    putz(0, 2 * NM + zm, si, false);
-                    putz(2, zm, s2, true);
-                    putz(2, NM + zm, c2, false);
-                    putz(2, 2 * NM + zm, s2, false);
+                    putz(0, zm, 0, -1.0f);
+                    putz(0, NM + zm, 1, 1.0f);
+                    putz(0, 2 * NM + zm, 0, 1.0f);
+                    putz(2, zm, 2, -1.0f);
+                    putz(2, NM + zm, 3, 1.0f);
+                    putz(2, 2 * NM + zm, 2, 1.0f);
                 }
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 mbar_arrive(&full_bar[s]);
@@ -495,24 +506,23 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                             break;
                         }
                         tc_fence_after();
-                        const uint32_t sb = smem_u32(ring + (size_t)s * G::STAGE);
+                        // descriptors are linear in the address field: the stage's base
+                        // descriptor plus the operand's offset in 16-byte units (shared
+                        // addresses stay below 2^18, so the 14-bit field never carries)
+                        const uint64_t sd0 = sdesc(smem_u32(ring + (size_t)s * G::STAGE));
                         const uint32_t acc0 = kb > kb0 ? 1u : 0u;
                         // one complex product: D += A_g (re, im) x Z window, split FP16
                         auto cplx = [&](uint32_t d, int ga, int zz) {
-                            const uint32_t ab = sb + (uint32_t)(4 * ga) * G::A_BYTES;
-                            const uint64_t arh = sdesc(ab), arl = sdesc(ab + G::A_BYTES);
-                            const uint64_t aih = sdesc(ab + 2 * G::A_BYTES);
-                            const uint64_t ail = sdesc(ab + 3 * G::A_BYTES);
-                            const uint32_t zb = sb + G::Z_OFF + (uint32_t)zz * G::Z_BYTES;
+                            const uint32_t ao = (uint32_t)(4 * ga) * G::A_BYTES;
+                            const uint64_t ad[4] = {sd0 + (ao >> 4), sd0 + ((ao + G::A_BYTES) >> 4),
+                                                    sd0 + ((ao + 2 * G::A_BYTES) >> 4),
+                                                    sd0 + ((ao + 3 * G::A_BYTES) >> 4)};
+                            const uint32_t zo = G::Z_OFF + (uint32_t)zz * G::Z_BYTES;
                             // [Br; Bi] = Z rows NM.., [-Bi; Br] = Z rows 0..
-                            const uint64_t bh = sdesc(zb + G::NM * 32), bl = sdesc(zb + G::Z_BYTES + G::NM * 32);
-                            const uint64_t nh = sdesc(zb), nl = sdesc(zb + G::Z_BYTES);
-                            mma_f16(d, arh, bh, idesc, acc0);
-                            mma_f16(d, arh, bl, idesc, 1u);
-                            mma_f16(d, arl, bh, idesc, 1u);
-                            mma_f16(d, aih, nh, idesc, 1u);
-                            mma_f16(d, aih, nl, idesc, 1u);
-                            mma_f16(d, ail, nh, idesc, 1u);
+                            const uint64_t bd[4] = {sd0 + ((zo + G::NM * 32) >> 4),
+                                                    sd0 + ((zo + G::Z_BYTES + G::NM * 32) >> 4),
+                                                    sd0 + (zo >> 4), sd0 + ((zo + G::Z_BYTES) >> 4)};
+                            mma_cplx6(d, ad, bd, idesc, acc0);
                         };
                         if (GEN) {
                             cplx(d0 + 0, 0, 0);                    // [C | S]

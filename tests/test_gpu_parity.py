@@ -228,6 +228,31 @@ def test_every_compiled_mixed_shape(eng, shape):
     assert check_best(r.best_idx, ref, tol=MIXED_ATOL) == []
 
 
+@pytest.mark.parametrize("variant", [0, 1])
+def test_tensor_form_is_deterministic(eng, variant):
+    """Repeated calls of the tensor-core form give bit-identical periodograms. This is what
+    showed a missing cross-proxy fence on the record ring: without it, a producer warp
+    occasionally read the next slot's records, and the affected objects (about one in 300)
+    changed from run to run by up to 0.07 in power."""
+    w = synth.lognormal_batch(seed=2000, n_freq=3000, error=bool(variant))
+    y = w.y
+    if variant:
+        _, y = pyoracle.batch_pgram(1, w.t, w.y, w.dy, w.offsets, w.fmin, w.df, n_freq=1)
+    saved = eng.get_tuning(variant)
+    try:
+        eng.set_tuning(variant, 32 if variant == 0 else 16, 128, 1, 3, 0)
+        runs = [eng.run_host(variant, "mixed", w.t, y, w.dy if variant else None, w.offsets,
+                             w.fmin, w.df, w.n_freq, normalize=(variant == 0),
+                             want_pgram=True).pgram.copy() for _ in range(4)]
+    finally:
+        eng.set_tuning(variant, *saved)
+    for r in runs[1:]:
+        assert np.array_equal(r, runs[0])
+    ref, _ = pyoracle.batch_pgram(variant, w.t, y, w.dy, w.offsets, w.fmin, w.df,
+                                  n_freq=w.n_freq, normalize=(variant == 0))
+    assert mixed_abs_err(runs[0], ref) < MIXED_ATOL
+
+
 @pytest.mark.parametrize("scale", [3.2, 1e3, 3e5, 4e8, 5e9])
 def test_plain_fp64_sincos_against_cuda(eng, scale):
     """The plain form's table-driven FP64 sine/cosine against CUDA's sincos(): both are
