@@ -368,7 +368,8 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                     float x0[2][4], x1[2][4], x2[2][4], x3[2][4], x4[2][4], x5[2][4];
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
-                        const bool valid = ja + (uint32_t)q < cnt;
+                        // observations past the object's end (clamped records, finite values)
+                        // are cancelled by zero Z entries, so A needs no mask
                         const uint64_t ph =
                             (uint64_t)ka * ra[q].z + (((uint64_t)ra[q].y << 32) | ra[q].x);
                         const uint32_t hi = (uint32_t)(ph >> 32) + ka * ra[q].w;
@@ -376,8 +377,8 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                         turn_sincos(hi, sn[0], cs[0]);
                         cs[1] = fmaf(cs[0], va[q].z, -sn[0] * va[q].w);  // rotate by s grid points
                         sn[1] = fmaf(sn[0], va[q].z, cs[0] * va[q].w);
-                        const float v0 = valid ? va[q].x * sc0 : 0.0f;
-                        const float v1 = valid ? va[q].y * sc1 : 0.0f;
+                        const float v0 = va[q].x * sc0;
+                        const float v1 = va[q].y * sc1;
 #pragma unroll
                         for (int rr = 0; rr < 2; ++rr) {
                             const float c2 = fmaf(cs[rr], cs[rr], -sn[rr] * sn[rr]);
@@ -390,8 +391,8 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                                 x4[rr][q] = v0 * c2;  // weighted doubled angle
                                 x5[rr][q] = v0 * s2;
                             } else {
-                                x2[rr][q] = valid ? c2 : 0.0f;
-                                x3[rr][q] = valid ? s2 : 0.0f;
+                                x2[rr][q] = c2;
+                                x3[rr][q] = s2;
                             }
                         }
                     }
@@ -428,10 +429,13 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                         const uint32_t hi = (uint32_t)(ph >> 32) + kb128 * rb[q].y;
                         float sn, cs;
                         turn_sincos(hi, sn, cs);
-                        cr[q] = cs;
-                        si[q] = sn;
-                        c2[q] = fmaf(cs, cs, -sn * sn);
-                        s2[q] = 2.0f * cs * sn;
+                        // zero for observations past the object's end: they cancel A's
+                        // entries of the clamped records in every product
+                        const float mk = zj + (uint32_t)q < cnt ? 1.0f : 0.0f;
+                        cr[q] = cs * mk;
+                        si[q] = sn * mk;
+                        c2[q] = fmaf(cs, cs, -sn * sn) * mk;
+                        s2[q] = 2.0f * cs * sn * mk;
                     }
                     // each value split once; -x = (-hi) + (-lo) exactly
                     float zh[4][2], zl[4][2];
