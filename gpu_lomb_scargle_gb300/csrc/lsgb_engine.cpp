@@ -356,7 +356,7 @@ struct lsgb_engine {
     DevBuf in_t, in_y, in_dy, out_pg, out_idx, out_p;
     // defaults measured fastest on the 999-object, 1e6-frequency batches: the tensor-core
     // form (lsgb_tensor.cu) for both variants
-    MixedShape shape[2] = {{32, 128, 1, 3, 0}, {16, 128, 1, 3, 0}};
+    MixedShape shape[2] = {{64, 128, 1, 3, 0}, {32, 128, 1, 3, 0}};
     uint32_t last_kernels = 0;
     uint64_t last_units = 0;
     cudaEvent_t ev_main0 = nullptr, ev_main1 = nullptr;  // around the last main-kernel launch

@@ -60,26 +60,30 @@ constexpr int kProducerWarp0 = 6;
 constexpr int kProducerThreads = 256;
 constexpr int kEpilogueThreads = 128;
 constexpr uint32_t kTmemCols = 512;
-constexpr uint32_t kBufCols = 128;   // TMEM columns of one partial buffer
-constexpr uint32_t kRunCol = 256;    // first TMEM column of the running sums
+constexpr uint32_t kBufCols = 128;   // TMEM columns of one partial buffer (two of them)
+constexpr uint32_t kRun0Col = 256;   // running sums of phase 0 (exp(i theta) sums)
+constexpr uint32_t kRun1Col = 384;   // running sums of phase 1 (exp(2i theta) sums)
 constexpr long long kWaitCycles = 1ll << 32;  // ~2 s at 2 GHz
 
 // Per-variant geometry.
 template <bool GEN>
 struct TGeo {
-    static constexpr int NM = GEN ? 16 : 32;       // coarse frequency steps m per unit
+    static constexpr int NM = GEN ? 32 : 64;       // coarse frequency steps m per unit
     static constexpr int N = 2 * NM;               // MMA N: [real | imaginary]
-    static constexpr int NAG = GEN ? 3 : 2;        // A groups: v e^ia (, v1 e^ia), (v) e^2ia
-    static constexpr int W = NAG * N;              // accumulator columns per unit
+    static constexpr int NAG0 = GEN ? 2 : 1;       // phase-0 A groups: v e^ia (, v1 e^ia)
+    static constexpr int W0 = NAG0 * N;            // phase-0 accumulator columns
+    static constexpr int W1 = N;                   // phase-1 accumulator columns
     static constexpr int A_BYTES = kTP * kTK * 2;  // one 128 x 16 FP16 matrix
     static constexpr int Z_ROWS = 3 * NM;
     static constexpr int Z_BYTES = Z_ROWS * kTK * 2;
-    // stage: A matrices (group g, re/im, hi/lo) then Z matrices (angle 1/2, hi/lo)
-    static constexpr int Z_OFF = NAG * 4 * A_BYTES;
-    static constexpr int STAGE = ((Z_OFF + 4 * Z_BYTES) + 1023) / 1024 * 1024;
-    static constexpr int STAGES = GEN ? 3 : 4;
+    // stage: A matrices (group g, re/im, hi/lo) then the Z matrix (hi, lo)
+    static constexpr int Z_OFF = NAG0 * 4 * A_BYTES;
+    static constexpr int STAGE = ((Z_OFF + 2 * Z_BYTES) + 1023) / 1024 * 1024;
+    static constexpr int STAGES = GEN ? 5 : 6;
     static constexpr int TILE = kTP * NM;          // frequencies per unit
-    static_assert(W <= (int)kBufCols, "partial buffer too narrow");
+    static_assert(W0 <= (int)kBufCols && W1 <= (int)kBufCols, "partial buffer too narrow");
+    static_assert(kRun1Col + W1 <= kTmemCols && kRun0Col + W0 <= kRun1Col, "TMEM layout");
+    static_assert(NM % 32 == 0, "Z rows in groups of 32 per producer thread");
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -314,6 +318,9 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
     tc_fence_after();
     const uint32_t tmem = s_tmem;
 
+    // Every role walks the same sequence: units b, b + grid, ...; in each unit phase 0
+    // (exp(i theta) sums) then phase 1 (exp(2i theta) sums), each over the unit's nkb
+    // K-blocks, cut into passes of kPassKB K-blocks.
     if (warp >= kProducerWarp0) {
         // ---------------- producers ----------------
         const uint32_t pw = (uint32_t)(warp - kProducerWarp0);  // 0..7
@@ -324,8 +331,9 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
         const uint32_t p = 16u * pw + (lane & 7u);
         const uint32_t ja = 8u * h + 4u * qd;
         const uint32_t offa0 = kmaj_off(p, ja), offa1 = kmaj_off(p + kTensorRowStep, ja);
-        // Z: row m, observations zj, zj+1 of K half zh; a warp writes 8 rows x 16 bytes
-        const bool zact = GEN ? pw < 4 : true;
+        // Z: rows m = zm + 32 i (i < ZM), observations zj, zj+1 of K half zh; a warp writes
+        // 8 rows x 16 bytes per store
+        constexpr int ZM = G::NM / 32;
         const uint32_t zm = 8u * (pw >> 1) + (lane >> 2);
         const uint32_t zh = pw & 1u;
         const uint32_t zj = 8u * zh + 2u * (lane & 3u);
@@ -335,7 +343,9 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             const uint32_t kT = w.tile * (uint32_t)G::TILE;
             const ObjInfo &ob = a.objs[w.o];
             const float sc0 = ob.tsc0, sc1 = ob.tsc1;
-            for (uint32_t kb = 0; kb < w.nkb; ++kb, ++g) {
+            for (uint32_t ks = 0; ks < 2u * w.nkb; ++ks, ++g) {
+                const bool ph1 = ks >= w.nkb;
+                const uint32_t kb = ph1 ? ks - w.nkb : ks;
                 const uint32_t r = g % kRecSlots, ur = g / kRecSlots;
                 const uint32_t s = g % S, us = g / S;
                 if (!mbar_wait(&rfull_bar[r], ur & 1u, &s_abort, a.status)) break;
@@ -364,12 +374,11 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                 // ---- A operands ----
                 {
                     const uint32_t ka = kT + p;
-                    // values [row][quantity][observation]
-                    float x0[2][4], x1[2][4], x2[2][4], x3[2][4], x4[2][4], x5[2][4];
+                    // values [row][quantity][observation]; observations past the object's
+                    // end (clamped records, finite values) are cancelled by zero Z entries
+                    float x0[2][4], x1[2][4], x2[2][4], x3[2][4];
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
-                        // observations past the object's end (clamped records, finite values)
-                        // are cancelled by zero Z entries, so A needs no mask
                         const uint64_t ph =
                             (uint64_t)ka * ra[q].z + (((uint64_t)ra[q].y << 32) | ra[q].x);
                         const uint32_t hi = (uint32_t)(ph >> 32) + ka * ra[q].w;
@@ -381,18 +390,19 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                         const float v1 = va[q].y * sc1;
 #pragma unroll
                         for (int rr = 0; rr < 2; ++rr) {
-                            const float c2 = fmaf(cs[rr], cs[rr], -sn[rr] * sn[rr]);
-                            const float s2 = 2.0f * cs[rr] * sn[rr];
-                            x0[rr][q] = v0 * cs[rr];
-                            x1[rr][q] = v0 * sn[rr];
-                            if (GEN) {
-                                x2[rr][q] = v1 * cs[rr];
-                                x3[rr][q] = v1 * sn[rr];
-                                x4[rr][q] = v0 * c2;  // weighted doubled angle
-                                x5[rr][q] = v0 * s2;
+                            if (!ph1) {
+                                x0[rr][q] = v0 * cs[rr];
+                                x1[rr][q] = v0 * sn[rr];
+                                if (GEN) {
+                                    x2[rr][q] = v1 * cs[rr];
+                                    x3[rr][q] = v1 * sn[rr];
+                                }
                             } else {
-                                x2[rr][q] = c2;
-                                x3[rr][q] = s2;
+                                const float c2 = fmaf(cs[rr], cs[rr], -sn[rr] * sn[rr]);
+                                const float s2 = 2.0f * cs[rr] * sn[rr];
+                                // doubled angle, weighted for the generalized variant
+                                x0[rr][q] = GEN ? v0 * c2 : c2;
+                                x1[rr][q] = GEN ? v0 * s2 : s2;
                             }
                         }
                     }
@@ -411,56 +421,52 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                     for (int rr = 0; rr < 2; ++rr) {
                         put4(0, rr, x0);
                         put4(2, rr, x1);
-                        put4(4, rr, x2);
-                        put4(6, rr, x3);
-                        if (GEN) {
-                            put4(8, rr, x4);
-                            put4(10, rr, x5);
+                        if (GEN && !ph1) {
+                            put4(4, rr, x2);
+                            put4(6, rr, x3);
                         }
                     }
                 }
-                // ---- Z operands: Z = [-Bi; Br; Bi] for the angles m beta and 2 m beta ----
-                if (zact) {
-                    float cr[2], si[2], c2[2], s2[2];
-                    const uint32_t kb128 = 128u * zm;
+                // ---- Z operands: Z = [-Bi; Br; Bi] for the angle m beta (phase 0) or
+                // 2 m beta (phase 1) ----
+                {
+                    float zh_[ZM][2][2], zl_[ZM][2][2];  // [m][cos / sin][observation]
 #pragma unroll
-                    for (int q = 0; q < 2; ++q) {
-                        const uint64_t ph = (uint64_t)kb128 * rb[q].x;
-                        const uint32_t hi = (uint32_t)(ph >> 32) + kb128 * rb[q].y;
-                        float sn, cs;
-                        turn_sincos(hi, sn, cs);
-                        // zero for observations past the object's end: they cancel A's
-                        // entries of the clamped records in every product
-                        const float mk = zj + (uint32_t)q < cnt ? 1.0f : 0.0f;
-                        cr[q] = cs * mk;
-                        si[q] = sn * mk;
-                        c2[q] = fmaf(cs, cs, -sn * sn) * mk;
-                        s2[q] = 2.0f * cs * sn * mk;
-                    }
-                    // each value split once; -x = (-hi) + (-lo) exactly
-                    float zh[4][2], zl[4][2];
+                    for (int i = 0; i < ZM; ++i) {
+                        const uint32_t kb128 = 128u * (zm + 32u * (uint32_t)i);
 #pragma unroll
-                    for (int q = 0; q < 2; ++q) {
-                        vsplit(si[q], zh[0][q], zl[0][q]);
-                        vsplit(cr[q], zh[1][q], zl[1][q]);
-                        vsplit(s2[q], zh[2][q], zl[2][q]);
-                        vsplit(c2[q], zh[3][q], zl[3][q]);
+                        for (int q = 0; q < 2; ++q) {
+                            const uint64_t ph = (uint64_t)kb128 * rb[q].x;
+                            const uint32_t hi = (uint32_t)(ph >> 32) + kb128 * rb[q].y;
+                            float sn, cs;
+                            turn_sincos(hi, sn, cs);
+                            if (ph1) {
+                                const float c2 = fmaf(cs, cs, -sn * sn);
+                                sn = 2.0f * cs * sn;
+                                cs = c2;
+                            }
+                            // zero for observations past the object's end: they cancel A's
+                            // entries of the clamped records in every product
+                            const float mk = zj + (uint32_t)q < cnt ? 1.0f : 0.0f;
+                            vsplit(cs * mk, zh_[i][0][q], zl_[i][0][q]);
+                            vsplit(sn * mk, zh_[i][1][q], zl_[i][1][q]);
+                        }
                     }
-                    auto putz = [&](int zmat, uint32_t row, int v, float sg) {
-                        unsigned char *base =
-                            st + G::Z_OFF + (size_t)zmat * G::Z_BYTES + kmaj_off(row, zj);
-                        *reinterpret_cast<uint32_t *>(base) = pack_h2(sg * zh[v][0], sg * zh[v][1]);
-                        *reinterpret_cast<uint32_t *>(base + G::Z_BYTES) =
-                            pack_h2(sg * zl[v][0], sg * zl[v][1]);
-                    };
-                    constexpr uint32_t NM = G::NM;
-                    // angle m beta: Z matrices 0 (hi), 1 (lo); 2 m beta: 2 (hi), 3 (lo)
-                    putz(0, zm, 0, -1.0f);
-                    putz(0, NM + zm, 1, 1.0f);
-                    putz(0, 2 * NM + zm, 0, 1.0f);
-                    putz(2, zm, 2, -1.0f);
-                    putz(2, NM + zm, 3, 1.0f);
-                    putz(2, 2 * NM + zm, 2, 1.0f);
+#pragma unroll
+                    for (int i = 0; i < ZM; ++i) {
+                        const uint32_t m = zm + 32u * (uint32_t)i;
+                        // -x = (-hi) + (-lo) exactly; Z matrices 0 (hi) and 1 (lo)
+                        auto putz = [&](uint32_t row, int v, float sg) {
+                            unsigned char *base = st + G::Z_OFF + kmaj_off(row, zj);
+                            *reinterpret_cast<uint32_t *>(base) =
+                                pack_h2(sg * zh_[i][v][0], sg * zh_[i][v][1]);
+                            *reinterpret_cast<uint32_t *>(base + G::Z_BYTES) =
+                                pack_h2(sg * zl_[i][v][0], sg * zl_[i][v][1]);
+                        };
+                        putz(m, 1, -1.0f);
+                        putz(G::NM + m, 0, 1.0f);
+                        putz(2 * G::NM + m, 1, 1.0f);
+                    }
                 }
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 mbar_arrive(&full_bar[s]);
@@ -473,7 +479,8 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             uint32_t g = 0;
             for (uint32_t u = blockIdx.x; u < units && !s_abort; u += gridDim.x) {
                 const UnitInfo w = unit_info(a, u);
-                for (uint32_t kb = 0; kb < w.nkb; ++kb, ++g) {
+                for (uint32_t ks = 0; ks < 2u * w.nkb; ++ks, ++g) {
+                    const uint32_t kb = ks >= w.nkb ? ks - w.nkb : ks;
                     const uint32_t r = g % kRecSlots, ur = g / kRecSlots;
                     if (!mbar_wait(&rempty_bar[r], (ur & 1u) ^ 1u, &s_abort, a.status)) break;
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -494,51 +501,48 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             bool ok = true;
             for (uint32_t u = blockIdx.x; u < units && ok; u += gridDim.x) {
                 const UnitInfo w = unit_info(a, u);
-                for (uint32_t kb0 = 0; kb0 < w.nkb && ok; kb0 += kPassKB, ++gp) {
-                    const uint32_t buf = gp & 1u, ub = gp >> 1;
-                    if (!mbar_wait(&pempty_bar[buf], (ub & 1u) ^ 1u, &s_abort, a.status)) {
-                        ok = false;
-                        break;
-                    }
-                    tc_fence_after();
-                    const uint32_t d0 = tmem + buf * kBufCols;
-                    const uint32_t kb1 = min(w.nkb, kb0 + (uint32_t)kPassKB);
-                    for (uint32_t kb = kb0; kb < kb1; ++kb, ++g) {
-                        const uint32_t s = g % S, use = g / S;
-                        if (!mbar_wait(&full_bar[s], use & 1u, &s_abort, a.status)) {
+                for (uint32_t ph = 0; ph < 2 && ok; ++ph) {
+                    for (uint32_t kb0 = 0; kb0 < w.nkb && ok; kb0 += kPassKB, ++gp) {
+                        const uint32_t buf = gp & 1u, ub = gp >> 1;
+                        if (!mbar_wait(&pempty_bar[buf], (ub & 1u) ^ 1u, &s_abort, a.status)) {
                             ok = false;
                             break;
                         }
                         tc_fence_after();
-                        // descriptors are linear in the address field: the stage's base
-                        // descriptor plus the operand's offset in 16-byte units (shared
-                        // addresses stay below 2^18, so the 14-bit field never carries)
-                        const uint64_t sd0 = sdesc(smem_u32(ring + (size_t)s * G::STAGE));
-                        const uint32_t acc0 = kb > kb0 ? 1u : 0u;
-                        // one complex product: D += A_g (re, im) x Z window, split FP16
-                        auto cplx = [&](uint32_t d, int ga, int zz) {
-                            const uint32_t ao = (uint32_t)(4 * ga) * G::A_BYTES;
-                            const uint64_t ad[4] = {sd0 + (ao >> 4), sd0 + ((ao + G::A_BYTES) >> 4),
-                                                    sd0 + ((ao + 2 * G::A_BYTES) >> 4),
-                                                    sd0 + ((ao + 3 * G::A_BYTES) >> 4)};
-                            const uint32_t zo = G::Z_OFF + (uint32_t)zz * G::Z_BYTES;
+                        const uint32_t d0 = tmem + buf * kBufCols;
+                        const uint32_t kb1 = min(w.nkb, kb0 + (uint32_t)kPassKB);
+                        for (uint32_t kb = kb0; kb < kb1; ++kb, ++g) {
+                            const uint32_t s = g % S, use = g / S;
+                            if (!mbar_wait(&full_bar[s], use & 1u, &s_abort, a.status)) {
+                                ok = false;
+                                break;
+                            }
+                            tc_fence_after();
+                            // descriptors are linear in the address field: the stage's base
+                            // descriptor plus the operand's offset in 16-byte units (shared
+                            // addresses stay below 2^18, so the 14-bit field never carries)
+                            const uint64_t sd0 = sdesc(smem_u32(ring + (size_t)s * G::STAGE));
+                            const uint32_t acc0 = kb > kb0 ? 1u : 0u;
                             // [Br; Bi] = Z rows NM.., [-Bi; Br] = Z rows 0..
-                            const uint64_t bd[4] = {sd0 + ((zo + G::NM * 32) >> 4),
-                                                    sd0 + ((zo + G::Z_BYTES + G::NM * 32) >> 4),
-                                                    sd0 + (zo >> 4), sd0 + ((zo + G::Z_BYTES) >> 4)};
-                            mma_cplx6(d, ad, bd, idesc, acc0);
-                        };
-                        if (GEN) {
-                            cplx(d0 + 0, 0, 0);                    // [C | S]
-                            cplx(d0 + (uint32_t)G::N, 1, 0);       // [YC | YS]
-                            cplx(d0 + 2u * (uint32_t)G::N, 2, 2);  // [C2 | S2]
-                        } else {
-                            cplx(d0 + 0, 0, 0);                    // [XC | XS]
-                            cplx(d0 + (uint32_t)G::N, 1, 2);       // [C2 | S2]
+                            const uint64_t bd[4] = {
+                                sd0 + ((G::Z_OFF + G::NM * 32) >> 4),
+                                sd0 + ((G::Z_OFF + G::Z_BYTES + G::NM * 32) >> 4),
+                                sd0 + (G::Z_OFF >> 4), sd0 + ((G::Z_OFF + G::Z_BYTES) >> 4)};
+                            // one complex product: D += A_g (re, im) x Z window, split FP16
+                            auto cplx = [&](uint32_t d, int ga) {
+                                const uint32_t ao = (uint32_t)(4 * ga) * G::A_BYTES;
+                                const uint64_t ad[4] = {
+                                    sd0 + (ao >> 4), sd0 + ((ao + G::A_BYTES) >> 4),
+                                    sd0 + ((ao + 2 * G::A_BYTES) >> 4),
+                                    sd0 + ((ao + 3 * G::A_BYTES) >> 4)};
+                                mma_cplx6(d, ad, bd, idesc, acc0);
+                            };
+                            cplx(d0, 0);  // [XC | XS], [C | S], or [C2 | S2]
+                            if (GEN && ph == 0) cplx(d0 + (uint32_t)G::N, 1);  // [YC | YS]
+                            mma_commit(&empty_bar[s]);
                         }
-                        mma_commit(&empty_bar[s]);
+                        if (ok) mma_commit(&pfull_bar[buf]);
                     }
-                    if (ok) mma_commit(&pfull_bar[buf]);
                 }
             }
             // every issued MMA has completed before TMEM is released
@@ -552,101 +556,105 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
         // ---------------- fold and epilogue (warps 0-3: TMEM lanes 32 warp ..) ----------------
         const uint32_t pl = (uint32_t)warp * 32u + (uint32_t)lane;
         const uint32_t lane_base = ((uint32_t)warp * 32u) << 16;
-        const uint32_t run = tmem + lane_base + kRunCol;
+        const uint32_t run1 = tmem + lane_base + kRun0Col, run2 = tmem + lane_base + kRun1Col;
         uint32_t gp = 0;
         bool ok = true;
         for (uint32_t u = blockIdx.x; u < units && ok; u += gridDim.x) {
             const UnitInfo w = unit_info(a, u);
             const uint32_t npass = (w.nkb + kPassKB - 1) / kPassKB;
-            for (uint32_t pi = 0; pi < npass; ++pi, ++gp) {
-                const uint32_t buf = gp & 1u, ub = gp >> 1;
-                if (!mbar_wait(&pfull_bar[buf], ub & 1u, &s_abort, a.status)) {
-                    ok = false;
-                    break;
-                }
-                tc_fence_after();
-                const uint32_t part = tmem + lane_base + buf * kBufCols;
-                // fold: running = (pi ? running : 0) + partial, 32 columns per round; the
-                // partial buffer is released as soon as it has been read
-                static_assert(G::W % 32 == 0, "fold in 32-column rounds");
+            for (uint32_t ph = 0; ph < 2 && ok; ++ph) {
+                const uint32_t run = ph ? run2 : run1;
+                const uint32_t wcols = ph ? (uint32_t)G::W1 : (uint32_t)G::W0;
+                for (uint32_t pi = 0; pi < npass; ++pi, ++gp) {
+                    const uint32_t buf = gp & 1u, ub = gp >> 1;
+                    if (!mbar_wait(&pfull_bar[buf], ub & 1u, &s_abort, a.status)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t part = tmem + lane_base + buf * kBufCols;
+                    // fold: running = (pi ? running : 0) + partial, 32 columns per round;
+                    // the partial buffer is released as soon as it has been read
 #pragma unroll 1
-                for (uint32_t c = 0; c < (uint32_t)G::W; c += 32) {
-                    uint32_t x[32], y[32];
-                    tmem_ld32(part + c, x);
-                    if (pi) tmem_ld32(run + c, y);
-                    tmem_wait_ld();
-                    if (pi) {
+                    for (uint32_t c = 0; c < wcols; c += 32) {
+                        uint32_t x[32], y[32];
+                        tmem_ld32(part + c, x);
+                        if (pi) tmem_ld32(run + c, y);
+                        tmem_wait_ld();
+                        if (pi) {
 #pragma unroll
-                        for (int i = 0; i < 32; ++i)
-                            x[i] = __float_as_uint(__uint_as_float(x[i]) + __uint_as_float(y[i]));
+                            for (int i = 0; i < 32; ++i)
+                                x[i] = __float_as_uint(__uint_as_float(x[i]) + __uint_as_float(y[i]));
+                        }
+                        tmem_st32(run + c, x);
                     }
-                    tmem_st32(run + c, x);
+                    tmem_wait_st();
+                    tc_fence_before();
+                    mbar_arrive(&pempty_bar[buf]);
                 }
-                tmem_wait_st();
-                tc_fence_before();
-                mbar_arrive(&pempty_bar[buf]);
-                if (pi + 1 < npass) continue;
-                // last pass: power from the running sums
-                const uint32_t kT = w.tile * (uint32_t)G::TILE;
-                const ObjInfo &ob = a.objs[w.o];
-                const float nrm = ob.norm32;
-                const float us0 = 1.0f / ob.tsc0, us1 = 1.0f / ob.tsc1;  // powers of two
-                const float Wt = __fdividef(1.0f, ob.invw32);
-                const float Nf = (float)w.n;
-                const uint64_t out0 = (uint64_t)w.o * a.n_freq;
-                float bp = 0.0f;
-                uint32_t bk = 0xffffffffu;
-                if (w.tile == 0 && pl == 0) bk = 0;  // the reference's (power 0, index 0) start
-                constexpr int NQ = 2 * G::NAG;       // quantities per frequency
+            }
+            if (!ok) break;
+            // power from the running sums of both phases
+            const uint32_t kT = w.tile * (uint32_t)G::TILE;
+            const ObjInfo &ob = a.objs[w.o];
+            const float nrm = ob.norm32;
+            const float us0 = 1.0f / ob.tsc0, us1 = 1.0f / ob.tsc1;  // powers of two
+            const float Wt = __fdividef(1.0f, ob.invw32);
+            const float Nf = (float)w.n;
+            const uint64_t out0 = (uint64_t)w.o * a.n_freq;
+            float bp = 0.0f;
+            uint32_t bk = 0xffffffffu;
+            if (w.tile == 0 && pl == 0) bk = 0;  // the reference's (power 0, index 0) start
+            // quantities: phase 0 groups (re, im) then phase 1 (re, im)
+            constexpr int NQ = GEN ? 6 : 4;
 #pragma unroll 1
-                for (int m0 = 0; m0 < G::NM; m0 += 8) {
-                    // all loads of the chunk first, one wait
-                    uint32_t x[NQ][8];
+            for (int m0 = 0; m0 < G::NM; m0 += 8) {
+                uint32_t x[NQ][8];
 #pragma unroll
-                    for (int k = 0; k < NQ; ++k) {
-                        // quantity k: group k/2, real (even k) or imaginary part
-                        const uint32_t col = (uint32_t)((k >> 1) * G::N + (k & 1) * G::NM + m0);
-                        tmem_ld8(run + col, x[k]);
+                for (int k = 0; k < NQ; ++k) {
+                    const bool p1 = k >= NQ - 2;
+                    const int kk = p1 ? k - (NQ - 2) : k;
+                    const uint32_t col = (uint32_t)((kk >> 1) * G::N + (kk & 1) * G::NM + m0);
+                    tmem_ld8((p1 ? run2 : run1) + col, x[k]);
+                }
+                tmem_wait_ld();
+                float q[NQ][8];
+#pragma unroll
+                for (int k = 0; k < NQ; ++k)
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) q[k][i] = __uint_as_float(x[k][i]);
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const uint32_t k = kT + pl + (uint32_t)kTP * (uint32_t)(m0 + i);
+                    float P;
+                    if (GEN) {
+                        // CC = (W + sum w cos 2t) / 2, CS = sum w sin 2t / 2, W = wsum_f
+                        P = gen_power_f(ob.invw32, ob.ybar32, q[0][i] * us0, q[1][i] * us0,
+                                        q[2][i] * us1, q[3][i] * us1,
+                                        0.5f * fmaf(q[4][i], us0, Wt), 0.5f * q[5][i] * us0) *
+                            nrm;
+                    } else {
+                        P = std_power_f(Nf, q[0][i] * us0, q[1][i] * us0, 0.5f * (Nf + q[2][i]),
+                                        0.5f * q[3][i]) *
+                            nrm;
                     }
-                    tmem_wait_ld();
-                    float q[NQ][8];
-#pragma unroll
-                    for (int k = 0; k < NQ; ++k)
-#pragma unroll
-                        for (int i = 0; i < 8; ++i) q[k][i] = __uint_as_float(x[k][i]);
-#pragma unroll
-                    for (int i = 0; i < 8; ++i) {
-                        const uint32_t k = kT + pl + (uint32_t)kTP * (uint32_t)(m0 + i);
-                        float P;
-                        if (GEN) {
-                            // CC = (W + sum w cos 2t) / 2, CS = sum w sin 2t / 2, W = wsum_f
-                            P = gen_power_f(ob.invw32, ob.ybar32, q[0][i] * us0, q[1][i] * us0,
-                                            q[2][i] * us1, q[3][i] * us1,
-                                            0.5f * fmaf(q[4][i], us0, Wt), 0.5f * q[5][i] * us0) *
-                                nrm;
-                        } else {
-                            P = std_power_f(Nf, q[0][i] * us0, q[1][i] * us0, 0.5f * (Nf + q[2][i]),
-                                            0.5f * q[3][i]) *
-                                nrm;
-                        }
-                        if (k < a.n_freq) {
-                            if (a.pgram) store_out<OutT>(a.pgram, out0 + k, P);
-                            if (better(P, k, bp, bk)) { bp = P; bk = k; }
-                        }
+                    if (k < a.n_freq) {
+                        if (a.pgram) store_out<OutT>(a.pgram, out0 + k, P);
+                        if (better(P, k, bp, bk)) { bp = P; bk = k; }
                     }
                 }
-                if (a.best_key) {
+            }
+            if (a.best_key) {
 #pragma unroll
-                    for (int off = 16; off > 0; off >>= 1) {
-                        const float op = __shfl_xor_sync(0xffffffffu, bp, off);
-                        const uint32_t ok2 = __shfl_xor_sync(0xffffffffu, bk, off);
-                        if (better(op, ok2, bp, bk)) { bp = op; bk = ok2; }
-                    }
-                    if (lane == 0 && bp > 0.0f)
-                        atomicMax(a.best_key + w.o,
-                                  ((unsigned long long)__float_as_uint(bp) << 32) |
-                                      (unsigned long long)(~bk));
+                for (int off = 16; off > 0; off >>= 1) {
+                    const float op = __shfl_xor_sync(0xffffffffu, bp, off);
+                    const uint32_t ok2 = __shfl_xor_sync(0xffffffffu, bk, off);
+                    if (better(op, ok2, bp, bk)) { bp = op; bk = ok2; }
                 }
+                if (lane == 0 && bp > 0.0f)
+                    atomicMax(a.best_key + w.o,
+                              ((unsigned long long)__float_as_uint(bp) << 32) |
+                                  (unsigned long long)(~bk));
             }
         }
     }

@@ -118,7 +118,7 @@ LSGB_API void lsgb_plan_destroy(lsgb_plan *plan);
  * 2 packed f32x2 over frequencies strided by the CTA width, advanced by the
  * second-order recurrence x[p+1] = 2 cos(phi) x[p] - x[p-1] where it is well
  * conditioned; 3 the tensor-core form, with F = coarse steps per unit and 128 threads
- * standing for its 128 fine steps: (32, 128, 1, 3, 0) standard and (16, 128, 1, 3, 0)
+ * standing for its 128 fine steps: (64, 128, 1, 3, 0) standard and (32, 128, 1, 3, 0)
  * generalized, the defaults), and two observations per loop iteration (1) or one (0).
  * 0 (-1 for the last two) keeps the current value. Returns LSGB_ERR_INVALID for shapes
  * that are not compiled in. */

@@ -240,7 +240,8 @@ def test_tensor_form_is_deterministic(eng, variant):
         _, y = pyoracle.batch_pgram(1, w.t, w.y, w.dy, w.offsets, w.fmin, w.df, n_freq=1)
     saved = eng.get_tuning(variant)
     try:
-        eng.set_tuning(variant, 32 if variant == 0 else 16, 128, 1, 3, 0)
+        shape = [sh for sh in E.mixed_shapes() if sh[0] == variant and sh[4] == 3][0]
+        eng.set_tuning(variant, *shape[1:])
         runs = [eng.run_host(variant, "mixed", w.t, y, w.dy if variant else None, w.offsets,
                              w.fmin, w.df, w.n_freq, normalize=(variant == 0),
                              want_pgram=True).pgram.copy() for _ in range(4)]
