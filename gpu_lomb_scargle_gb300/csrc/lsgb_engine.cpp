@@ -83,11 +83,12 @@ void two_prod(double a, double b_hi, double b_lo, double &hi, double &lo) {
 // Device buffers one batch needs besides the caller's arrays.
 struct Workspace {
     DevBuf objs, offs, perm, rec, tile_best, counter, keys;
+    DevBuf ztab;  // tensor form: per-object right operands (tensor_ztab_bytes)
     // sticky error word of the tensor-form kernel (a bounded pipeline wait that timed
     // out); zeroed when allocated and after it is reported
     DevBuf status;
     void release() {
-        DevBuf *b[] = {&objs, &offs, &perm, &rec, &tile_best, &counter, &keys, &status};
+        DevBuf *b[] = {&objs, &offs, &perm, &rec, &tile_best, &counter, &keys, &ztab, &status};
         for (DevBuf *x : b) x->release();
     }
 };
@@ -101,6 +102,7 @@ struct Batch {
     uint32_t *best_idx = nullptr;
     uint32_t n_obj = 0, n_freq = 0, n_tiles = 0, max_n = 0, chunk = 0;
     uint64_t rows = 0, units = 0;
+    uint64_t total_kb = 0;  // tensor form: K-blocks of the batch (Z table entries per phase)
     double fmin = 0, df = 0;
     MixedShape shape{};
     uint32_t reanchor = 0;
@@ -190,6 +192,13 @@ int plan_batch(Batch &b, int sms, const MixedShape *shapes, uint32_t reanchor, i
         b.fold = false;
         b.smem = tensor_smem_bytes(variant);
         occ = 1;
+        uint64_t kb = 0;
+        for (uint32_t o = 0; o < n_obj; ++o) {
+            b.objs[o].kb0 = (uint32_t)kb;
+            kb += (b.objs[o].n + kTensorKBlock - 1) / kTensorKBlock;
+        }
+        if (kb >= 0xffffffffull) return fail(LSGB_ERR_INVALID, "batch too long for the tensor form");
+        b.total_kb = kb;
     } else if (mixed) {
         // Shared memory per CTA: at most what keeps the CTAs per SM that the shape's
         // register budget allows resident (less the per-CTA reservation and the static
@@ -233,6 +242,7 @@ int upload_tables(const Batch &b, Workspace &ws, cudaStream_t st) {
     if (b.want_best && !mixed) LSGB_CUDA(ws.tile_best.ensure(sizeof(TileBest) * b.units));
     if (b.want_best && mixed) LSGB_CUDA(ws.keys.ensure(sizeof(unsigned long long) * b.n_obj));
     if (mixed) LSGB_CUDA(ws.rec.ensure(mixed_global_rec_bytes(b.shape) * b.rows));
+    if (mixed && b.shape.x2 == 3) LSGB_CUDA(ws.ztab.ensure(tensor_ztab_bytes(b.variant, b.total_kb)));
     if (mixed && !ws.status.p) {
         LSGB_CUDA(ws.status.ensure(sizeof(uint32_t)));
         LSGB_CUDA(cudaMemsetAsync(ws.status.p, 0, sizeof(uint32_t), st));
@@ -289,6 +299,7 @@ int enqueue_batch(Batch &b, Workspace &ws, cudaStream_t st, cudaEvent_t ev0, cud
         ++kernels;
         MixedArgs a{};
         a.rec = ws.rec.p;
+        a.ztab = ws.ztab.p;
         a.objs = d_objs;
         a.perm = (const uint32_t *)ws.perm.p;
         a.n_obj = b.n_obj;
@@ -302,6 +313,10 @@ int enqueue_batch(Batch &b, Workspace &ws, cudaStream_t st, cudaEvent_t ev0, cud
         a.reanchor = b.reanchor;
         a.fold = b.fold ? 1u : 0u;
         a.status = (uint32_t *)ws.status.p;
+        if (b.shape.x2 == 3) {
+            LSGB_CUDA(launch_tensor_ztab(b.variant, a, b.total_kb, st));
+            ++kernels;
+        }
         if (ev0) LSGB_CUDA(record(ev0, st, capturing));
         LSGB_CUDA(launch_mixed(b.variant, b.dtype, b.shape, a, b.grid, b.smem, st));
         if (ev1) LSGB_CUDA(record(ev1, st, capturing));
@@ -663,6 +678,9 @@ LSGB_API int lsgb_periodogram_host(lsgb_engine *eng, int variant, int precision,
             LSGB_CUDA(eng->ws.keys.ensure(sizeof(unsigned long long) * n_obj));
             if (precision == LSGB_MIXED)
                 LSGB_CUDA(eng->ws.rec.ensure(mixed_global_rec_bytes(eng->shape[variant]) * rows));
+            if (precision == LSGB_MIXED && eng->shape[variant].x2 == 3)
+                LSGB_CUDA(eng->ws.ztab.ensure(
+                    tensor_ztab_bytes(variant, rows / kTensorKBlock + n_obj)));
             else if (best_idx || best_power)
                 LSGB_CUDA(eng->ws.tile_best.ensure(sizeof(TileBest) * max_tiles * n_obj));
         }

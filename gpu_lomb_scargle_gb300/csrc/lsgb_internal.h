@@ -49,7 +49,8 @@ constexpr double kSecondOrderMinSin = 0.125;
 struct ObjInfo {
     uint64_t row0;  // first row of the object in t / y / dy / records
     uint32_t n;     // rows
-    uint32_t pad;
+    uint32_t kb0;   // tensor form: the object's first K-block in the Z table (the sum of
+                    // ceil(n / 16) over the preceding objects)
     double norm;    // standard: 2/(N var(y)) or 1; generalized mixed: 1 / weighted var(y)
     double wtot;    // generalized: sum of 1/dy^2
     double ymean;   // generalized: sum(y/dy^2) / sum(1/dy^2)
@@ -94,6 +95,8 @@ struct MixedArgs {
                            // (objects longer than `chunk` fold their chunk sums into it)
     uint32_t *status;      // tensor form: bit 0 set when a bounded pipeline wait timed out
                            // (may be null)
+    const void *ztab;      // tensor form: the Z table (tensor_ztab_bytes), filled by
+                           // launch_tensor_ztab for this batch
 };
 
 
@@ -151,6 +154,13 @@ cudaError_t mixed_occupancy(int variant, int dtype, MixedShape shape, size_t sme
 uint32_t tensor_tile_freqs(int variant);
 size_t tensor_smem_bytes(int variant);
 cudaError_t launch_tensor(int variant, int dtype, const MixedArgs &a, int grid, cudaStream_t st);
+// The tensor form's Z table: for every K-block (16 observations) of every object and both
+// phases, the tile-independent right operand exp(i m beta) (phase 0) or exp(2i m beta)
+// (phase 1), split into FP16 hi / lo matrices in the kernel's shared-memory layout.
+// total_kb = sum over objects of ceil(n / 16); ObjInfo::kb0 must hold the prefix sums.
+constexpr uint32_t kTensorKBlock = 16;
+size_t tensor_ztab_bytes(int variant, uint64_t total_kb);
+cudaError_t launch_tensor_ztab(int variant, const MixedArgs &a, uint64_t total_kb, cudaStream_t st);
 // Compiled mixed shapes as (variant, F, threads, min CTAs, packed, unroll); returns the count.
 int mixed_shapes(int *out, int max_shapes);
 cudaError_t launch_plain(int variant, int in_dtype, int out_dtype, const PlainArgs &a, int grid,

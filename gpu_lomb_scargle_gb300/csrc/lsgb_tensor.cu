@@ -33,7 +33,10 @@
 //   warp 4      TMEM allocation and the MMA issuer (one thread);
 //   warp 5      record loader (one thread): bulk copies of 16 ObsRec per K-block into a
 //               shared-memory ring;
-//   warps 6-13  producers: the split FP16 operands of one K-block (16 observations) per
+//   warp 14     Z loader (one thread): bulk copies of the K-block's right operand from
+//               the Z table (zgen_kernel, once per batch: it does not depend on the
+//               frequency tile) into the operand stage;
+//   warps 6-13  producers: the split FP16 left operands of one K-block (16 observations) per
 //               stage of a shared-memory ring, K-major without swizzle. A thread computes
 //               A rows p and p + kTensorRowStep, the second by rotating the first with
 //               the record's (cd, sd), so half the A entries need no SFU sine/cosine.
@@ -55,7 +58,8 @@ constexpr int kTK = 16;         // observations per K-block (the FP16 MMA depth)
 constexpr int kPassKB = 4;      // K-blocks accumulated in TMEM before an FP32 fold
 constexpr int kRecSlots = 8;    // record ring depth (K-blocks)
 constexpr int kRecSlotBytes = kTK * 32;
-constexpr int kThreads = 448;   // 14 warps
+constexpr int kThreads = 480;   // 15 warps
+constexpr int kZLoaderWarp = 14;
 constexpr int kProducerWarp0 = 6;
 constexpr int kProducerThreads = 256;
 constexpr int kEpilogueThreads = 128;
@@ -291,7 +295,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
 
     if (tid == 0) {
         for (int s = 0; s < S; ++s) {
-            mbar_init(&full_bar[s], kProducerThreads);
+            mbar_init(&full_bar[s], kProducerThreads + 1);  // + the Z loader's bytes
             mbar_init(&empty_bar[s], 1);
         }
         for (int r = 0; r < kRecSlots; ++r) {
@@ -321,7 +325,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
     // Every role walks the same sequence: units b, b + grid, ...; in each unit phase 0
     // (exp(i theta) sums) then phase 1 (exp(2i theta) sums), each over the unit's nkb
     // K-blocks, cut into passes of kPassKB K-blocks.
-    if (warp >= kProducerWarp0) {
+    if (warp >= kProducerWarp0 && warp < kZLoaderWarp) {
         // ---------------- producers ----------------
         const uint32_t pw = (uint32_t)(warp - kProducerWarp0);  // 0..7
         // A: rows p and p + kTensorRowStep (the second by the record's rotation), the
@@ -331,12 +335,6 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
         const uint32_t p = 16u * pw + (lane & 7u);
         const uint32_t ja = 8u * h + 4u * qd;
         const uint32_t offa0 = kmaj_off(p, ja), offa1 = kmaj_off(p + kTensorRowStep, ja);
-        // Z: rows m = zm + 32 i (i < ZM), observations zj, zj+1 of K half zh; a warp writes
-        // 8 rows x 16 bytes per store
-        constexpr int ZM = G::NM / 32;
-        const uint32_t zm = 8u * (pw >> 1) + (lane >> 2);
-        const uint32_t zh = pw & 1u;
-        const uint32_t zj = 8u * zh + 2u * (lane & 3u);
         uint32_t g = 0;
         for (uint32_t u = blockIdx.x; u < units && !s_abort; u += gridDim.x) {
             const UnitInfo w = unit_info(a, u);
@@ -358,12 +356,6 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                     const uint32_t jj = min(ja + (uint32_t)q, cnt - 1u);
                     ra[q] = *reinterpret_cast<const uint4 *>(rs + 32u * jj);
                     va[q] = *reinterpret_cast<const float4 *>(rs + 32u * jj + 16u);
-                }
-                uint2 rb[2];
-#pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                    const uint32_t jj = min(zj + (uint32_t)q, cnt - 1u);
-                    rb[q] = *reinterpret_cast<const uint2 *>(rs + 32u * jj + 8u);
                 }
                 // the slot's next bulk copy is an async-proxy write: order these
                 // generic-proxy reads before it (write-after-read across proxies)
@@ -427,51 +419,31 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                         }
                     }
                 }
-                // ---- Z operands: Z = [-Bi; Br; Bi] for the angle m beta (phase 0) or
-                // 2 m beta (phase 1) ----
-                {
-                    float zh_[ZM][2][2], zl_[ZM][2][2];  // [m][cos / sin][observation]
-#pragma unroll
-                    for (int i = 0; i < ZM; ++i) {
-                        const uint32_t kb128 = 128u * (zm + 32u * (uint32_t)i);
-#pragma unroll
-                        for (int q = 0; q < 2; ++q) {
-                            const uint64_t ph = (uint64_t)kb128 * rb[q].x;
-                            const uint32_t hi = (uint32_t)(ph >> 32) + kb128 * rb[q].y;
-                            float sn, cs;
-                            turn_sincos(hi, sn, cs);
-                            if (ph1) {
-                                const float c2 = fmaf(cs, cs, -sn * sn);
-                                sn = 2.0f * cs * sn;
-                                cs = c2;
-                            }
-                            // zero for observations past the object's end: they cancel A's
-                            // entries of the clamped records in every product
-                            const float mk = zj + (uint32_t)q < cnt ? 1.0f : 0.0f;
-                            vsplit(cs * mk, zh_[i][0][q], zl_[i][0][q]);
-                            vsplit(sn * mk, zh_[i][1][q], zl_[i][1][q]);
-                        }
-                    }
-#pragma unroll
-                    for (int i = 0; i < ZM; ++i) {
-                        const uint32_t m = zm + 32u * (uint32_t)i;
-                        // -x = (-hi) + (-lo) exactly; Z matrices 0 (hi) and 1 (lo)
-                        auto putz = [&](uint32_t row, int v, float sg) {
-                            unsigned char *base = st + G::Z_OFF + kmaj_off(row, zj);
-                            *reinterpret_cast<uint32_t *>(base) =
-                                pack_h2(sg * zh_[i][v][0], sg * zh_[i][v][1]);
-                            *reinterpret_cast<uint32_t *>(base + G::Z_BYTES) =
-                                pack_h2(sg * zl_[i][v][0], sg * zl_[i][v][1]);
-                        };
-                        putz(m, 1, -1.0f);
-                        putz(G::NM + m, 0, 1.0f);
-                        putz(2 * G::NM + m, 1, 1.0f);
-                    }
-                }
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 mbar_arrive(&full_bar[s]);
             }
         }
+    } else if (warp == kZLoaderWarp) {
+        // ---------------- Z loader: the unit's right operands from the Z table ----------------
+        if (lane == 0) {
+            const unsigned char *zt = static_cast<const unsigned char *>(a.ztab);
+            uint32_t g = 0;
+            for (uint32_t u = blockIdx.x; u < units && !s_abort; u += gridDim.x) {
+                const UnitInfo w = unit_info(a, u);
+                const uint32_t kb0 = a.objs[w.o].kb0;
+                for (uint32_t ks = 0; ks < 2u * w.nkb; ++ks, ++g) {
+                    const uint32_t ph = ks >= w.nkb ? 1u : 0u;
+                    const uint32_t kb = ph ? ks - w.nkb : ks;
+                    const uint32_t s = g % S, us = g / S;
+                    if (!mbar_wait(&empty_bar[s], (us & 1u) ^ 1u, &s_abort, a.status)) break;
+                    mbar_expect_tx(&full_bar[s], 2u * G::Z_BYTES);
+                    bulk_copy_g2s(ring + (size_t)s * G::STAGE + G::Z_OFF,
+                                  zt + ((uint64_t)(kb0 + kb) * 2u + ph) * 2u * G::Z_BYTES,
+                                  2u * G::Z_BYTES, &full_bar[s]);
+                }
+            }
+        }
+        __syncwarp();
     } else if (warp == 5) {
         // ---------------- record loader ----------------
         if (lane == 0) {
@@ -669,6 +641,65 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
     }
 }
 
+// The Z table: one CTA per (K-block, phase) builds the two Z matrices (hi, lo) of
+// Z = [-Bi; Br; Bi], B[m][j] = exp(i m beta_j) (phase 0) or exp(2i m beta_j) (phase 1), in
+// shared memory with the layout the tensor kernel stages, and copies them out coalesced.
+// Observations past the object's end get zero entries, which cancel the A side's entries
+// of the clamped records in every product.
+template <bool GEN>
+__global__ void __launch_bounds__(256) zgen_kernel(MixedArgs a, uint32_t total_kb) {
+    using G = TGeo<GEN>;
+    __shared__ __align__(16) unsigned char zs[2 * G::Z_BYTES];
+    const uint32_t kbg = blockIdx.x >> 1, ph = blockIdx.x & 1u;
+    if (kbg >= total_kb) return;
+    // the object of this K-block: the last o with kb0 <= kbg
+    uint32_t lo = 0, hi = a.n_obj;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (a.objs[mid].kb0 <= kbg) lo = mid; else hi = mid;
+    }
+    const ObjInfo &ob = a.objs[lo];
+    const uint32_t kb = kbg - ob.kb0;
+    const uint32_t cnt = min((uint32_t)kTK, ob.n - kb * kTK);
+    const ObsRec *rec = static_cast<const ObsRec *>(a.rec) + ob.row0 + (uint64_t)kb * kTK;
+    for (uint32_t e = threadIdx.x; e < (uint32_t)G::NM * (kTK / 2); e += blockDim.x) {
+        const uint32_t m = e / (kTK / 2), j0 = 2u * (e % (kTK / 2));
+        const uint32_t k128 = 128u * m;
+        float h[2][2], l[2][2];  // [cos / sin][observation]
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const uint32_t j = j0 + (uint32_t)q;
+            const ObsRec &r = rec[min(j, cnt - 1u)];
+            const uint64_t pz = (uint64_t)k128 * r.b_lo;
+            const uint32_t t32 = (uint32_t)(pz >> 32) + k128 * r.b_hi;
+            float sn, cs;
+            turn_sincos(t32, sn, cs);
+            if (ph) {
+                const float c2 = fmaf(cs, cs, -sn * sn);
+                sn = 2.0f * cs * sn;
+                cs = c2;
+            }
+            const float mk = j < cnt ? 1.0f : 0.0f;
+            vsplit(cs * mk, h[0][q], l[0][q]);
+            vsplit(sn * mk, h[1][q], l[1][q]);
+        }
+        // -x = (-hi) + (-lo) exactly; hi matrix then lo matrix
+        auto putz = [&](uint32_t row, int v, float sg) {
+            unsigned char *base = zs + kmaj_off(row, j0);
+            *reinterpret_cast<uint32_t *>(base) = pack_h2(sg * h[v][0], sg * h[v][1]);
+            *reinterpret_cast<uint32_t *>(base + G::Z_BYTES) = pack_h2(sg * l[v][0], sg * l[v][1]);
+        };
+        putz(m, 1, -1.0f);
+        putz(G::NM + m, 0, 1.0f);
+        putz(2 * G::NM + m, 1, 1.0f);
+    }
+    __syncthreads();
+    uint4 *dst = reinterpret_cast<uint4 *>(const_cast<void *>(a.ztab)) +
+                 ((uint64_t)kbg * 2u + ph) * (2u * G::Z_BYTES / 16u);
+    const uint4 *src = reinterpret_cast<const uint4 *>(zs);
+    for (uint32_t i = threadIdx.x; i < 2u * G::Z_BYTES / 16u; i += blockDim.x) dst[i] = src[i];
+}
+
 template <bool GEN>
 size_t tensor_smem() {
     return (size_t)TGeo<GEN>::STAGES * TGeo<GEN>::STAGE + (size_t)kRecSlots * kRecSlotBytes + 1024;
@@ -691,6 +722,22 @@ uint32_t tensor_tile_freqs(int variant) {
 }
 
 size_t tensor_smem_bytes(int variant) { return variant ? tensor_smem<true>() : tensor_smem<false>(); }
+
+size_t tensor_ztab_bytes(int variant, uint64_t total_kb) {
+    return (size_t)total_kb * 2u * 2u *
+           (size_t)(variant ? TGeo<true>::Z_BYTES : TGeo<false>::Z_BYTES);
+}
+
+cudaError_t launch_tensor_ztab(int variant, const MixedArgs &a, uint64_t total_kb, cudaStream_t st) {
+    if (total_kb == 0) return cudaSuccess;
+    const uint64_t blocks = total_kb * 2u;
+    if (blocks > 0x7fffffffull) return cudaErrorInvalidValue;
+    if (variant == 0)
+        zgen_kernel<false><<<(unsigned)blocks, 256, 0, st>>>(a, (uint32_t)total_kb);
+    else
+        zgen_kernel<true><<<(unsigned)blocks, 256, 0, st>>>(a, (uint32_t)total_kb);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_tensor(int variant, int dtype, const MixedArgs &a, int grid, cudaStream_t st) {
     if (variant == 0)
