@@ -21,21 +21,26 @@ __device__ __forceinline__ bool better(V p1, uint32_t k1, V p2, uint32_t k2) {
 //   P = 1/2 [ (Q+U)/(N+r) + (Q-U)/(N-r) ],  Q = XC^2+XS^2,
 //   U = [ (CC-SS)(XC^2-XS^2) + 4 CS XC XS ] / r,  r = hypot(CC-SS, 2 CS),
 // which is source/main.cu:1588-1598 with cos/sin(2 omega tau) = (CC-SS, 2CS)/r.
-// N - r is evaluated as 4 (CC SS - CS^2)/(N + r) to avoid cancellation.
-__device__ __forceinline__ float fast_sqrt(float h) { return h > 0.0f ? h * rsqrtf(h) : 0.0f; }
-
+// N - r is evaluated as 4 (CC SS - CS^2)/(N + r) to avoid cancellation, so with
+// d1 = N + r, d4 = 4 (CC SS - CS^2) and t = 1/(d1 d4):
+//   P = 1/2 [ (Q+U) (d4 t) + (Q-U) d1 (d1 t) ],
+// the factors d4 t = 1/d1 and d1 t = 1/(N - r) formed before they meet Q, U. Two SFU
+// operations: one reciprocal square root (1/r, and r = h/sqrt(h)) and one reciprocal.
 __device__ __forceinline__ float std_power_f(float N, float xc, float xs, float cc, float cs) {
     const float ss = N - cc;
     const float D = cc - ss;
     const float E = 2.0f * cs;
-    const float r = fast_sqrt(fmaf(D, D, E * E));
+    const float h = fmaf(D, D, E * E);
+    const float ir = h > 0.0f ? rsqrtf(h) : 0.0f;  // 1/r
+    const float r = h * ir;
     const float xc2 = xc * xc, xs2 = xs * xs;
     const float Q = xc2 + xs2;
     const float V = xc2 - xs2;
-    const float U = r > 0.0f ? __fdividef(fmaf(D, V, 2.0f * E * xc * xs), r) : V;
-    const float den1 = N + r;
-    const float den2 = __fdividef(4.0f * fmaf(cc, ss, -cs * cs), den1);
-    return 0.5f * (__fdividef(Q + U, den1) + __fdividef(Q - U, den2));
+    const float U = h > 0.0f ? fmaf(D, V, 2.0f * E * xc * xs) * ir : V;
+    const float d1 = N + r;
+    const float d4 = 4.0f * fmaf(cc, ss, -cs * cs);
+    const float t = __fdividef(1.0f, d1 * d4);
+    return 0.5f * fmaf(Q + U, d4 * t, (Q - U) * (d1 * (d1 * t)));
 }
 
 // Generalized (floating-mean) power from weighted sums with total weight W:
@@ -53,13 +58,16 @@ __device__ __forceinline__ float gen_power_f(float invW, float ybar, float C, fl
     const float vss = fmaf(-sb, sb, ss);
     const float vcs = fmaf(-cb, sb, cs);
     const float D = vcc - vss, E = 2.0f * vcs, T = vcc + vss;
-    const float r = fast_sqrt(fmaf(D, D, E * E));
+    const float h = fmaf(D, D, E * E);
+    const float ir = h > 0.0f ? rsqrtf(h) : 0.0f;  // 1/r
+    const float r = h * ir;
     const float yc2 = yc * yc, ys2 = ys * ys;
     const float Q = yc2 + ys2, V = yc2 - ys2;
-    const float U = r > 0.0f ? __fdividef(fmaf(D, V, 2.0f * E * yc * ys), r) : V;
-    const float den1 = T + r;
-    const float den2 = __fdividef(4.0f * fmaf(vcc, vss, -vcs * vcs), den1);
-    return __fdividef(Q + U, den1) + __fdividef(Q - U, den2);
+    const float U = h > 0.0f ? fmaf(D, V, 2.0f * E * yc * ys) * ir : V;
+    const float d1 = T + r;
+    const float d4 = 4.0f * fmaf(vcc, vss, -vcs * vcs);
+    const float t = __fdividef(1.0f, d1 * d4);
+    return fmaf(Q + U, d4 * t, (Q - U) * (d1 * (d1 * t)));
 }
 
 template <typename OutT>

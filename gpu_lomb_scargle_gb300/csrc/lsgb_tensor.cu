@@ -579,9 +579,10 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             if (w.tile == 0 && pl == 0) bk = 0;  // the reference's (power 0, index 0) start
             // quantities: phase 0 groups (re, im) then phase 1 (re, im)
             constexpr int NQ = GEN ? 6 : 4;
-#pragma unroll 1
-            for (int m0 = 0; m0 < G::NM; m0 += 8) {
-                uint32_t x[NQ][8];
+            // the standard variant loads chunk m0 + 8 while it computes chunk m0
+            constexpr bool PREFETCH = !GEN;
+            uint32_t x[NQ][8];
+            auto load_chunk = [&](int m0) {
 #pragma unroll
                 for (int k = 0; k < NQ; ++k) {
                     const bool p1 = k >= NQ - 2;
@@ -589,12 +590,18 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                     const uint32_t col = (uint32_t)((kk >> 1) * G::N + (kk & 1) * G::NM + m0);
                     tmem_ld8((p1 ? run2 : run1) + col, x[k]);
                 }
+            };
+            if (PREFETCH) load_chunk(0);
+#pragma unroll 1
+            for (int m0 = 0; m0 < G::NM; m0 += 8) {
+                if (!PREFETCH) load_chunk(m0);
                 tmem_wait_ld();
                 float q[NQ][8];
 #pragma unroll
                 for (int k = 0; k < NQ; ++k)
 #pragma unroll
                     for (int i = 0; i < 8; ++i) q[k][i] = __uint_as_float(x[k][i]);
+                if (PREFETCH && m0 + 8 < G::NM) load_chunk(m0 + 8);
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
                     const uint32_t k = kT + pl + (uint32_t)kTP * (uint32_t)(m0 + i);
