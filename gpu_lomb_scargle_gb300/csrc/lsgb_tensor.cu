@@ -28,8 +28,9 @@
 // the powers from the running sums.
 //
 // One persistent CTA per SM, warp-specialized:
-//   warps 0-3   fold and epilogue: TMEM lanes 32w.. (the lanes warp w may access), power
-//               per frequency, periodogram store, per-object maximum;
+//   warps 0-3, 15-18  fold and epilogue, two warps per TMEM lane quarter (warp w may
+//               access lanes 32 (w % 4) ..): power per frequency, periodogram store,
+//               per-object maximum;
 //   warp 4      TMEM allocation and the MMA issuer (one thread);
 //   warp 5      record loader (one thread): bulk copies of 16 ObsRec per K-block into a
 //               shared-memory ring;
@@ -58,11 +59,11 @@ constexpr int kTK = 16;         // observations per K-block (the FP16 MMA depth)
 constexpr int kPassKB = 4;      // K-blocks accumulated in TMEM before an FP32 fold
 constexpr int kRecSlots = 8;    // record ring depth (K-blocks)
 constexpr int kRecSlotBytes = kTK * 32;
-constexpr int kThreads = 480;   // 15 warps
+constexpr int kThreads = 608;   // 19 warps
 constexpr int kZLoaderWarp = 14;
 constexpr int kProducerWarp0 = 6;
 constexpr int kProducerThreads = 256;
-constexpr int kEpilogueThreads = 128;
+constexpr int kEpilogueThreads = 256;  // warps 0-3 and 15-18
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kBufCols = 128;   // TMEM columns of one partial buffer (two of them)
 constexpr uint32_t kRun0Col = 256;   // running sums of phase 0 (exp(i theta) sums)
@@ -222,6 +223,25 @@ __device__ __forceinline__ void tmem_st8(uint32_t taddr, const float (&v)[8]) {
         "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
         "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
         "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
+        : "memory");
+}
+// 16 consecutive accumulator columns (asynchronous until tmem_wait_ld).
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t *r) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+        "%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+          "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t *v) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+        "%13,%14,%15,%16};" ::"r"(taddr),
+        "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]),
+        "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]),
+        "r"(v[15])
         : "memory");
 }
 // 32 consecutive accumulator columns (asynchronous until tmem_wait_ld).
@@ -525,9 +545,14 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
         }
         __syncwarp();
     } else {
-        // ---------------- fold and epilogue (warps 0-3: TMEM lanes 32 warp ..) ----------------
-        const uint32_t pl = (uint32_t)warp * 32u + (uint32_t)lane;
-        const uint32_t lane_base = ((uint32_t)warp * 32u) << 16;
+        // ---------------- fold and epilogue (warps 0-3 and 15-18) ----------------
+        // warp w may access TMEM lanes 32 (w % 4) ..; the two warps of a lane quarter split
+        // the coarse steps: warp half eh owns m in [eh NM/2, (eh+1) NM/2), i.e. the same
+        // half of every NM-column quantity block, in the folds and in the power pass, so a
+        // warp only ever reads running sums it wrote itself
+        const uint32_t eq = (uint32_t)warp & 3u, eh = warp >= 15 ? 1u : 0u;
+        const uint32_t pl = eq * 32u + (uint32_t)lane;
+        const uint32_t lane_base = (eq * 32u) << 16;
         const uint32_t run1 = tmem + lane_base + kRun0Col, run2 = tmem + lane_base + kRun1Col;
         uint32_t gp = 0;
         bool ok = true;
@@ -545,20 +570,31 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                     }
                     tc_fence_after();
                     const uint32_t part = tmem + lane_base + buf * kBufCols;
-                    // fold: running = (pi ? running : 0) + partial, 32 columns per round;
-                    // the partial buffer is released as soon as it has been read
+                    // fold: running = (pi ? running : 0) + partial over this warp's half
+                    // of each quantity block; the partial buffer is released as soon as
+                    // both warps of the quarter have read it
+                    constexpr uint32_t HALF = G::NM / 2;
+                    static_assert(HALF == 32 || HALF == 16, "fold rounds of 32 or 16 columns");
 #pragma unroll 1
-                    for (uint32_t c = 0; c < wcols; c += 32) {
-                        uint32_t x[32], y[32];
-                        tmem_ld32(part + c, x);
-                        if (pi) tmem_ld32(run + c, y);
+                    for (uint32_t c = HALF * eh; c < wcols; c += G::NM) {
+                        uint32_t x[HALF], y[HALF];
+                        if (HALF == 32) {
+                            tmem_ld32(part + c, *reinterpret_cast<uint32_t(*)[32]>(x));
+                            if (pi) tmem_ld32(run + c, *reinterpret_cast<uint32_t(*)[32]>(y));
+                        } else {
+                            tmem_ld16(part + c, x);
+                            if (pi) tmem_ld16(run + c, y);
+                        }
                         tmem_wait_ld();
                         if (pi) {
 #pragma unroll
-                            for (int i = 0; i < 32; ++i)
+                            for (uint32_t i = 0; i < HALF; ++i)
                                 x[i] = __float_as_uint(__uint_as_float(x[i]) + __uint_as_float(y[i]));
                         }
-                        tmem_st32(run + c, x);
+                        if (HALF == 32)
+                            tmem_st32(run + c, *reinterpret_cast<const uint32_t(*)[32]>(x));
+                        else
+                            tmem_st16(run + c, x);
                     }
                     tmem_wait_st();
                     tc_fence_before();
@@ -576,7 +612,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             const uint64_t out0 = (uint64_t)w.o * a.n_freq;
             float bp = 0.0f;
             uint32_t bk = 0xffffffffu;
-            if (w.tile == 0 && pl == 0) bk = 0;  // the reference's (power 0, index 0) start
+            if (w.tile == 0 && pl == 0 && eh == 0) bk = 0;  // the reference's (power 0, index 0) start
             // quantities: phase 0 groups (re, im) then phase 1 (re, im)
             constexpr int NQ = GEN ? 6 : 4;
             // the standard variant loads chunk m0 + 8 while it computes chunk m0
@@ -591,9 +627,10 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                     tmem_ld8((p1 ? run2 : run1) + col, x[k]);
                 }
             };
-            if (PREFETCH) load_chunk(0);
+            const int mbeg = (int)eh * (G::NM / 2), mend = mbeg + G::NM / 2;
+            if (PREFETCH) load_chunk(mbeg);
 #pragma unroll 1
-            for (int m0 = 0; m0 < G::NM; m0 += 8) {
+            for (int m0 = mbeg; m0 < mend; m0 += 8) {
                 if (!PREFETCH) load_chunk(m0);
                 tmem_wait_ld();
                 float q[NQ][8];
@@ -601,7 +638,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                 for (int k = 0; k < NQ; ++k)
 #pragma unroll
                     for (int i = 0; i < 8; ++i) q[k][i] = __uint_as_float(x[k][i]);
-                if (PREFETCH && m0 + 8 < G::NM) load_chunk(m0 + 8);
+                if (PREFETCH && m0 + 8 < mend) load_chunk(m0 + 8);
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
                     const uint32_t k = kT + pl + (uint32_t)kTP * (uint32_t)(m0 + i);
