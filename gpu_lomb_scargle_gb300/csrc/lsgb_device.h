@@ -43,6 +43,52 @@ __device__ __forceinline__ float std_power_f(float N, float xc, float xs, float 
     return 0.5f * fmaf(Q + U, d4 * t, (Q - U) * (d1 * (d1 * t)));
 }
 
+// Twice the standard power from the raw sums XC, XS (of v e^{i theta}) and C2, S2 (of
+// e^{2 i theta}) of N observations, N2 = N^2. With cc = (N + C2)/2, ss = (N - C2)/2 and
+// cs = S2/2 the quantities of std_power_f reduce to D = C2, E = S2 and
+// d4 = 4 (cc ss - cs^2) = N^2 - (C2^2 + S2^2) = N^2 - h.
+__device__ __forceinline__ float std_power2_sums(float N, float N2, float xc, float xs,
+                                                 float c2, float s2) {
+    const float h = fmaf(c2, c2, s2 * s2);
+    const float ir = h > 0.0f ? rsqrtf(h) : 0.0f;  // 1/r
+    const float r = h * ir;
+    const float xc2 = xc * xc;
+    const float Q = fmaf(xs, xs, xc2);
+    const float V = fmaf(-xs, xs, xc2);
+    const float xs2 = xs + xs;
+    const float U = h > 0.0f ? fmaf(c2, V, (s2 * xc) * xs2) * ir : V;
+    const float d1 = N + r;
+    const float d4 = N2 - h;
+    const float t = __fdividef(1.0f, d1 * d4);
+    return fmaf(Q + U, d4 * t, (Q - U) * (d1 * (d1 * t)));
+}
+
+// Generalized power from weight-normalized sums: cb, sb = C/W, S/W; yc, ys the centered
+// YC/W - ybar cb, YS/W - ybar sb; c2, s2 = C2/W, S2/W (sums of w e^{2 i theta}). The
+// covariances of gen_power_f reduce to D = vcc - vss = c2 - cb^2 + sb^2,
+// E = 2 vcs = s2 - 2 cb sb, T = vcc + vss = 1 - cb^2 - sb^2 and
+// d4 = 4 (vcc vss - vcs^2) = T^2 - (D^2 + E^2).
+__device__ __forceinline__ float gen_power_sums(float cb, float sb, float yc, float ys, float c2,
+                                                float s2) {
+    const float cb2 = cb * cb, sb2 = sb * sb;
+    const float D = (c2 - cb2) + sb2;
+    const float m = cb * sb;
+    const float E = fmaf(-2.0f, m, s2);
+    const float T = (1.0f - cb2) - sb2;
+    const float h = fmaf(D, D, E * E);
+    const float ir = h > 0.0f ? rsqrtf(h) : 0.0f;  // 1/r
+    const float r = h * ir;
+    const float yc2 = yc * yc;
+    const float Q = fmaf(ys, ys, yc2);
+    const float V = fmaf(-ys, ys, yc2);
+    const float ys2 = ys + ys;
+    const float U = h > 0.0f ? fmaf(D, V, (E * yc) * ys2) * ir : V;
+    const float d1 = T + r;
+    const float d4 = fmaf(T, T, -h);
+    const float t = __fdividef(1.0f, d1 * d4);
+    return fmaf(Q + U, d4 * t, (Q - U) * (d1 * (d1 * t)));
+}
+
 // Generalized (floating-mean) power from weighted sums with total weight W:
 // the same closed form applied to the weighted covariances, which is
 // source/main.cu:1728-1776 with the second pass expressed by rotating the

@@ -153,9 +153,8 @@ __device__ __forceinline__ bool mbar_test(uint64_t *b, uint32_t parity) {
 
 // Waits for the phase of `parity` of barrier b. Returns false (and raises the CTA's
 // abort flag and the launch's status) on a timeout or when another role aborted.
-__device__ __noinline__ bool mbar_wait(uint64_t *b, uint32_t parity, volatile uint32_t *abort,
-                                       uint32_t *status) {
-    if (mbar_test(b, parity)) return true;
+__device__ __noinline__ bool mbar_wait_slow(uint64_t *b, uint32_t parity,
+                                            volatile uint32_t *abort, uint32_t *status) {
     const long long t0 = clock64();
     for (uint32_t it = 1;; ++it) {
         if (mbar_test(b, parity)) return true;
@@ -168,6 +167,11 @@ __device__ __noinline__ bool mbar_wait(uint64_t *b, uint32_t parity, volatile ui
             }
         }
     }
+}
+// The completed case inline, the polling loop out of line.
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, volatile uint32_t *abort,
+                                          uint32_t *status) {
+    return mbar_test(b, parity) || mbar_wait_slow(b, parity, abort, status);
 }
 
 __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes,
@@ -216,14 +220,6 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
                    "=r"(r[6]), "=r"(r[7])
                  : "r"(taddr));
-}
-__device__ __forceinline__ void tmem_st8(uint32_t taddr, const float (&v)[8]) {
-    asm volatile(
-        "tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr),
-        "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
-        "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
-        "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
-        : "memory");
 }
 // 16 consecutive accumulator columns (asynchronous until tmem_wait_ld).
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t *r) {
@@ -285,16 +281,37 @@ struct UnitInfo {
     uint64_t row0;
 };
 
-__device__ __forceinline__ UnitInfo unit_info(const MixedArgs &a, uint32_t u) {
+__device__ __forceinline__ UnitInfo unit_info_of(const MixedArgs &a, uint32_t u, uint32_t o) {
     UnitInfo w;
-    const uint32_t oi = u / a.n_tiles;
-    w.o = a.perm[oi];
-    w.tile = u - oi * a.n_tiles;
-    w.row0 = a.objs[w.o].row0;
-    w.n = a.objs[w.o].n;
+    w.o = o;
+    w.tile = u % a.n_tiles;
+    w.row0 = a.objs[o].row0;
+    w.n = a.objs[o].n;
     w.nkb = (w.n + kTK - 1) / kTK;
     return w;
 }
+
+// A CTA's walk over its units b, b + g, b + 2g, ... (b = blockIdx.x, g = gridDim.x) with
+// loads issued one unit ahead: next(u) returns unit u's information, loaded during the
+// previous call, then issues the object loads of unit u + g (whose object index was read
+// one call earlier still) and the object index of unit u + 2g. No role then waits on the
+// perm -> objs load chain at a unit boundary.
+struct UnitWalk {
+    UnitInfo nxt;
+    uint32_t o1;  // object of the unit after the one in nxt
+    __device__ __forceinline__ UnitWalk(const MixedArgs &a, uint32_t units) {
+        const uint32_t b = blockIdx.x, g = gridDim.x;
+        if (b < units) nxt = unit_info_of(a, b, a.perm[b / a.n_tiles]);
+        o1 = b + g < units ? a.perm[(b + g) / a.n_tiles] : 0u;
+    }
+    __device__ __forceinline__ UnitInfo next(const MixedArgs &a, uint32_t u, uint32_t units) {
+        const UnitInfo cur = nxt;
+        const uint32_t u1 = u + gridDim.x, u2 = u1 + gridDim.x;
+        if (u1 < units) nxt = unit_info_of(a, u1, o1);
+        o1 = u2 < units ? a.perm[u2 / a.n_tiles] : 0u;
+        return cur;
+    }
+};
 
 template <bool GEN, typename OutT>
 __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
@@ -356,8 +373,9 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
         const uint32_t ja = 8u * h + 4u * qd;
         const uint32_t offa0 = kmaj_off(p, ja), offa1 = kmaj_off(p + kTensorRowStep, ja);
         uint32_t g = 0;
+        UnitWalk walk(a, units);
         for (uint32_t u = blockIdx.x; u < units && !s_abort; u += gridDim.x) {
-            const UnitInfo w = unit_info(a, u);
+            const UnitInfo w = walk.next(a, u, units);
             const uint32_t kT = w.tile * (uint32_t)G::TILE;
             const ObjInfo &ob = a.objs[w.o];
             const float sc0 = ob.tsc0, sc1 = ob.tsc1;
@@ -448,8 +466,9 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
         if (lane == 0) {
             const unsigned char *zt = static_cast<const unsigned char *>(a.ztab);
             uint32_t g = 0;
+            UnitWalk walk(a, units);
             for (uint32_t u = blockIdx.x; u < units && !s_abort; u += gridDim.x) {
-                const UnitInfo w = unit_info(a, u);
+                const UnitInfo w = walk.next(a, u, units);
                 const uint32_t kb0 = a.objs[w.o].kb0;
                 for (uint32_t ks = 0; ks < 2u * w.nkb; ++ks, ++g) {
                     const uint32_t ph = ks >= w.nkb ? 1u : 0u;
@@ -469,8 +488,9 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
         if (lane == 0) {
             const ObsRec *rec = static_cast<const ObsRec *>(a.rec);
             uint32_t g = 0;
+            UnitWalk walk(a, units);
             for (uint32_t u = blockIdx.x; u < units && !s_abort; u += gridDim.x) {
-                const UnitInfo w = unit_info(a, u);
+                const UnitInfo w = walk.next(a, u, units);
                 for (uint32_t ks = 0; ks < 2u * w.nkb; ++ks, ++g) {
                     const uint32_t kb = ks >= w.nkb ? ks - w.nkb : ks;
                     const uint32_t r = g % kRecSlots, ur = g / kRecSlots;
@@ -491,8 +511,9 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             constexpr uint32_t idesc = idesc_f16(kTP, G::N);
             uint32_t g = 0, gp = 0;
             bool ok = true;
+            UnitWalk walk(a, units);
             for (uint32_t u = blockIdx.x; u < units && ok; u += gridDim.x) {
-                const UnitInfo w = unit_info(a, u);
+                const UnitInfo w = walk.next(a, u, units);
                 for (uint32_t ph = 0; ph < 2 && ok; ++ph) {
                     for (uint32_t kb0 = 0; kb0 < w.nkb && ok; kb0 += kPassKB, ++gp) {
                         const uint32_t buf = gp & 1u, ub = gp >> 1;
@@ -556,8 +577,13 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
         const uint32_t run1 = tmem + lane_base + kRun0Col, run2 = tmem + lane_base + kRun1Col;
         uint32_t gp = 0;
         bool ok = true;
+        UnitWalk walk(a, units);
         for (uint32_t u = blockIdx.x; u < units && ok; u += gridDim.x) {
-            const UnitInfo w = unit_info(a, u);
+            const UnitInfo w = walk.next(a, u, units);
+            // the object's fields for the power pass, loaded before the folds
+            const ObjInfo &ob = a.objs[w.o];
+            const float nrm = ob.norm32, tsc0 = ob.tsc0, tsc1 = ob.tsc1;
+            const float invw = ob.invw32, ybar = ob.ybar32;
             const uint32_t npass = (w.nkb + kPassKB - 1) / kPassKB;
             for (uint32_t ph = 0; ph < 2 && ok; ++ph) {
                 const uint32_t run = ph ? run2 : run1;
@@ -604,11 +630,12 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             if (!ok) break;
             // power from the running sums of both phases
             const uint32_t kT = w.tile * (uint32_t)G::TILE;
-            const ObjInfo &ob = a.objs[w.o];
-            const float nrm = ob.norm32;
-            const float us0 = 1.0f / ob.tsc0, us1 = 1.0f / ob.tsc1;  // powers of two
-            const float Wt = __fdividef(1.0f, ob.invw32);
-            const float Nf = (float)w.n;
+            const float us0 = 1.0f / tsc0, us1 = 1.0f / tsc1;  // powers of two
+            // standard: P = (2P of the raw sums) us0 (us0 nrm / 2), the scale applied in
+            // two steps so that us0^2 never forms; generalized: weight-normalized sums
+            const float fa = us0, fb = 0.5f * nrm * us0;
+            const float s0 = us0 * invw, s1 = us1 * invw;
+            const float Nf = (float)w.n, N2 = Nf * Nf;
             const uint64_t out0 = (uint64_t)w.o * a.n_freq;
             float bp = 0.0f;
             uint32_t bk = 0xffffffffu;
@@ -644,19 +671,20 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                     const uint32_t k = kT + pl + (uint32_t)kTP * (uint32_t)(m0 + i);
                     float P;
                     if (GEN) {
-                        // CC = (W + sum w cos 2t) / 2, CS = sum w sin 2t / 2, W = wsum_f
-                        P = gen_power_f(ob.invw32, ob.ybar32, q[0][i] * us0, q[1][i] * us0,
-                                        q[2][i] * us1, q[3][i] * us1,
-                                        0.5f * fmaf(q[4][i], us0, Wt), 0.5f * q[5][i] * us0) *
+                        const float cb = q[0][i] * s0, sb = q[1][i] * s0;
+                        P = gen_power_sums(cb, sb, fmaf(-ybar, cb, q[2][i] * s1),
+                                           fmaf(-ybar, sb, q[3][i] * s1), q[4][i] * s0,
+                                           q[5][i] * s0) *
                             nrm;
                     } else {
-                        P = std_power_f(Nf, q[0][i] * us0, q[1][i] * us0, 0.5f * (Nf + q[2][i]),
-                                        0.5f * q[3][i]) *
-                            nrm;
+                        P = (std_power2_sums(Nf, N2, q[0][i], q[1][i], q[2][i], q[3][i]) * fa) * fb;
                     }
+                    // a thread visits its frequencies in increasing k, so a strictly larger
+                    // power is the only way to displace its current best (ties keep the
+                    // lower index, as the reference's argmax does)
                     if (k < a.n_freq) {
                         if (a.pgram) store_out<OutT>(a.pgram, out0 + k, P);
-                        if (better(P, k, bp, bk)) { bp = P; bk = k; }
+                        if (P > bp) { bp = P; bk = k; }
                     }
                 }
             }
