@@ -83,12 +83,12 @@ void two_prod(double a, double b_hi, double b_lo, double &hi, double &lo) {
 // Device buffers one batch needs besides the caller's arrays.
 struct Workspace {
     DevBuf objs, offs, perm, rec, tile_best, counter, keys;
-    DevBuf ztab;  // tensor form: per-object right operands (tensor_ztab_bytes)
+    DevBuf optab;  // tensor form: per-K-block left operands and steps (tensor_optab_bytes)
     // sticky error word of the tensor-form kernel (a bounded pipeline wait that timed
     // out); zeroed when allocated and after it is reported
     DevBuf status;
     void release() {
-        DevBuf *b[] = {&objs, &offs, &perm, &rec, &tile_best, &counter, &keys, &ztab, &status};
+        DevBuf *b[] = {&objs, &offs, &perm, &rec, &tile_best, &counter, &keys, &optab, &status};
         for (DevBuf *x : b) x->release();
     }
 };
@@ -102,7 +102,7 @@ struct Batch {
     uint32_t *best_idx = nullptr;
     uint32_t n_obj = 0, n_freq = 0, n_tiles = 0, max_n = 0, chunk = 0;
     uint64_t rows = 0, units = 0;
-    uint64_t total_kb = 0;  // tensor form: K-blocks of the batch (Z table entries per phase)
+    uint64_t total_kb = 0;  // tensor form: K-blocks of the batch (operand table entries)
     double fmin = 0, df = 0;
     MixedShape shape{};
     uint32_t reanchor = 0;
@@ -242,7 +242,7 @@ int upload_tables(const Batch &b, Workspace &ws, cudaStream_t st) {
     if (b.want_best && !mixed) LSGB_CUDA(ws.tile_best.ensure(sizeof(TileBest) * b.units));
     if (b.want_best && mixed) LSGB_CUDA(ws.keys.ensure(sizeof(unsigned long long) * b.n_obj));
     if (mixed) LSGB_CUDA(ws.rec.ensure(mixed_global_rec_bytes(b.shape) * b.rows));
-    if (mixed && b.shape.x2 == 3) LSGB_CUDA(ws.ztab.ensure(tensor_ztab_bytes(b.variant, b.total_kb)));
+    if (mixed && b.shape.x2 == 3) LSGB_CUDA(ws.optab.ensure(tensor_optab_bytes(b.variant, b.total_kb)));
     if (mixed && !ws.status.p) {
         LSGB_CUDA(ws.status.ensure(sizeof(uint32_t)));
         LSGB_CUDA(cudaMemsetAsync(ws.status.p, 0, sizeof(uint32_t), st));
@@ -294,12 +294,11 @@ int enqueue_batch(Batch &b, Workspace &ws, cudaStream_t st, cudaEvent_t ev0, cud
         two_prod(b.df, kInv2PiHi, kInv2PiLo, g.df_hi, g.df_lo);
         LSGB_CUDA(launch_records(b.variant, b.dtype, b.t, b.y, b.dy, (const uint64_t *)ws.offs.p,
                                  b.n_obj, d_objs, b.rows, g, ws.rec.p,
-                                 b.shape.x2 == 2 ? (uint32_t)b.shape.nt : 0u,
-                                 b.shape.x2 == 3 ? kTensorRowStep : 1u, st));
+                                 b.shape.x2 == 2 ? (uint32_t)b.shape.nt : 0u, st));
         ++kernels;
         MixedArgs a{};
         a.rec = ws.rec.p;
-        a.ztab = ws.ztab.p;
+        a.optab = ws.optab.p;
         a.objs = d_objs;
         a.perm = (const uint32_t *)ws.perm.p;
         a.n_obj = b.n_obj;
@@ -314,7 +313,7 @@ int enqueue_batch(Batch &b, Workspace &ws, cudaStream_t st, cudaEvent_t ev0, cud
         a.fold = b.fold ? 1u : 0u;
         a.status = (uint32_t *)ws.status.p;
         if (b.shape.x2 == 3) {
-            LSGB_CUDA(launch_tensor_ztab(b.variant, a, b.total_kb, st));
+            LSGB_CUDA(launch_tensor_optab(b.variant, a, b.total_kb, st));
             ++kernels;
         }
         if (ev0) LSGB_CUDA(record(ev0, st, capturing));
@@ -679,8 +678,8 @@ LSGB_API int lsgb_periodogram_host(lsgb_engine *eng, int variant, int precision,
             if (precision == LSGB_MIXED)
                 LSGB_CUDA(eng->ws.rec.ensure(mixed_global_rec_bytes(eng->shape[variant]) * rows));
             if (precision == LSGB_MIXED && eng->shape[variant].x2 == 3)
-                LSGB_CUDA(eng->ws.ztab.ensure(
-                    tensor_ztab_bytes(variant, rows / kTensorKBlock + n_obj)));
+                LSGB_CUDA(eng->ws.optab.ensure(
+                    tensor_optab_bytes(variant, rows / kTensorKBlock + n_obj)));
             else if (best_idx || best_power)
                 LSGB_CUDA(eng->ws.tile_best.ensure(sizeof(TileBest) * max_tiles * n_obj));
         }

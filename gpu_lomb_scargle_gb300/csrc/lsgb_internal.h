@@ -12,7 +12,7 @@ namespace lsgb {
 //   f0 = fmin / 2pi and dfturn = df / 2pi, so the phase of grid point k is
 //   a + k*b (mod 2^64), exact to ~(1+k) * 2^-64 turns;
 //   cd, sd = cos, sin(2 pi s b): the rotation by s grid points (s = 1 for the
-//   recurrence loops, kTensorRowStep for the tensor form);
+//   recurrence loops; the tensor form does not use them);
 //   standard:    v0 = y,          v1 = 0
 //   generalized: v0 = w / W,      v1 = (w / W) * (y - ybar_w),   w = 1/dy^2.
 struct __align__(16) ObsRec {
@@ -49,7 +49,7 @@ constexpr double kSecondOrderMinSin = 0.125;
 struct ObjInfo {
     uint64_t row0;  // first row of the object in t / y / dy / records
     uint32_t n;     // rows
-    uint32_t kb0;   // tensor form: the object's first K-block in the Z table (the sum of
+    uint32_t kb0;   // tensor form: the object's first K-block in the operand table (the sum of
                     // ceil(n / 16) over the preceding objects)
     double norm;    // standard: 2/(N var(y)) or 1; generalized mixed: 1 / weighted var(y)
     double wtot;    // generalized: sum of 1/dy^2
@@ -95,8 +95,8 @@ struct MixedArgs {
                            // (objects longer than `chunk` fold their chunk sums into it)
     uint32_t *status;      // tensor form: bit 0 set when a bounded pipeline wait timed out
                            // (may be null)
-    const void *ztab;      // tensor form: the Z table (tensor_ztab_bytes), filled by
-                           // launch_tensor_ztab for this batch
+    const void *optab;     // tensor form: the operand table (tensor_optab_bytes), filled
+                           // by launch_tensor_optab for this batch
 };
 
 
@@ -133,17 +133,14 @@ inline size_t mixed_fold_bytes(int variant, const MixedShape &s) {
 // ---- launchers (lsgb_kernels.cu); all asynchronous on `st` ----
 cudaError_t launch_stats(int variant, int mixed, int dtype, int normalize, const void *y,
                          const void *dy, ObjInfo *objs, uint32_t n_obj, cudaStream_t st);
-// so_stride 0: ObsRec records whose (cd, sd) step is obs_step grid points (1 for the
-// rotation loops, kTensorRowStep for the tensor form); > 0: SoRec records for a
+// so_stride 0: ObsRec records whose (cd, sd) step is one grid point (the rotation loops;
+// the tensor form reads only a, b, v0, v1); > 0: SoRec records for a
 // second-order shape whose CTA has so_stride threads. `rec` holds rows x 32 or rows x 96
 // bytes accordingly.
 cudaError_t launch_records(int variant, int dtype, const void *t, const void *y, const void *dy,
                            const uint64_t *offsets, uint32_t n_obj, const ObjInfo *objs,
                            uint64_t rows, GridTurns g, void *rec, uint32_t so_stride,
-                           uint32_t obs_step, cudaStream_t st);
-// Grid-point distance of the two A rows a tensor-form producer thread computes (the second
-// by rotating the first with the record's (cd, sd)).
-constexpr uint32_t kTensorRowStep = 8;
+                           cudaStream_t st);
 // Mixed kernel: returns cudaErrorInvalidValue when (variant, dtype, shape) is not compiled.
 cudaError_t launch_mixed(int variant, int dtype, MixedShape shape, const MixedArgs &a,
                          int grid, size_t smem, cudaStream_t st);
@@ -154,13 +151,14 @@ cudaError_t mixed_occupancy(int variant, int dtype, MixedShape shape, size_t sme
 uint32_t tensor_tile_freqs(int variant);
 size_t tensor_smem_bytes(int variant);
 cudaError_t launch_tensor(int variant, int dtype, const MixedArgs &a, int grid, cudaStream_t st);
-// The tensor form's Z table: for every K-block (16 observations) of every object and both
-// phases, the tile-independent right operand exp(i m beta) (phase 0) or exp(2i m beta)
-// (phase 1), split into FP16 hi / lo matrices in the kernel's shared-memory layout.
+// The tensor form's operand table: for every K-block (16 observations) of every object and
+// both phases, the tile-independent left operand v exp(i (a + p b)) (phase 0) or
+// (v) exp(2i (a + p b)) (phase 1) for p < 128, split into FP16 hi / lo matrices in the
+// kernel's shared-memory layout, and the K-block's frequency steps b. Needs the records.
 // total_kb = sum over objects of ceil(n / 16); ObjInfo::kb0 must hold the prefix sums.
 constexpr uint32_t kTensorKBlock = 16;
-size_t tensor_ztab_bytes(int variant, uint64_t total_kb);
-cudaError_t launch_tensor_ztab(int variant, const MixedArgs &a, uint64_t total_kb, cudaStream_t st);
+size_t tensor_optab_bytes(int variant, uint64_t total_kb);
+cudaError_t launch_tensor_optab(int variant, const MixedArgs &a, uint64_t total_kb, cudaStream_t st);
 // Compiled mixed shapes as (variant, F, threads, min CTAs, packed, unroll); returns the count.
 int mixed_shapes(int *out, int max_shapes);
 cudaError_t launch_plain(int variant, int in_dtype, int out_dtype, const PlainArgs &a, int grid,

@@ -218,7 +218,7 @@ __global__ void stats_kernel(int variant, int mixed, int dtype, int normalize, c
 __global__ void records_kernel(int variant, int dtype, const void *t, const void *y,
                                const void *dy, const uint64_t *offsets, uint32_t n_obj,
                                const ObjInfo *objs, uint64_t rows, GridTurns g, void *rec,
-                               uint32_t so_stride, uint32_t obs_step) {
+                               uint32_t so_stride) {
     for (uint64_t row = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; row < rows;
          row += (uint64_t)gridDim.x * blockDim.x) {
         const double td = load_in(dtype, t, row);
@@ -226,7 +226,7 @@ __global__ void records_kernel(int variant, int dtype, const void *t, const void
         const uint64_t b = frac_turns_u64(g.df_hi, g.df_lo, td);
         // the step of the recurrence: one grid point, or so_stride of them (exact in the
         // fixed-point turns; the signed reading puts the angle in [-pi, pi))
-        const uint64_t bs = b * (uint64_t)(so_stride ? so_stride : obs_step);
+        const uint64_t bs = b * (uint64_t)(so_stride ? so_stride : 1u);
         double sd, cd;
         sincos((double)(long long)bs * kTwoPiOver2p64, &sd, &cd);
         ObsRec r;
@@ -1000,12 +1000,12 @@ cudaError_t launch_stats(int variant, int mixed, int dtype, int normalize, const
 cudaError_t launch_records(int variant, int dtype, const void *t, const void *y, const void *dy,
                            const uint64_t *offsets, uint32_t n_obj, const ObjInfo *objs,
                            uint64_t rows, GridTurns g, void *rec, uint32_t so_stride,
-                           uint32_t obs_step, cudaStream_t st) {
+                           cudaStream_t st) {
     if (rows == 0) return cudaSuccess;
     const uint64_t blocks64 = (rows + 255) / 256;
     const int blocks = (int)(blocks64 < 65535ull * 16 ? blocks64 : 65535ull * 16);
     records_kernel<<<blocks, 256, 0, st>>>(variant, dtype, t, y, dy, offsets, n_obj, objs, rows, g,
-                                           rec, so_stride, obs_step ? obs_step : 1u);
+                                           rec, so_stride);
     return cudaGetLastError();
 }
 

@@ -180,7 +180,7 @@ extern "C" LSGB_API int lsgb_periodogram_noalloc(int variant, int dtype, const v
     GridTurns g;
     two_prod(fmin, g.f0_hi, g.f0_lo);
     two_prod(df, g.df_hi, g.df_lo);
-    if ((e = launch_records(variant, dtype, t, y, dy, d_offs, n_obj, d_objs, rows, g, d_rec, 0u, 1u, st)) !=
+    if ((e = launch_records(variant, dtype, t, y, dy, d_offs, n_obj, d_objs, rows, g, d_rec, 0u, st)) !=
         cudaSuccess)
         return fail_cuda("records kernel", e);
     const uint32_t chunk = std::min<uint32_t>(max_n, kMixedSmemMax / (uint32_t)mixed_rec_bytes(shape));

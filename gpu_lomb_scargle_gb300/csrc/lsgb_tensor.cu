@@ -4,20 +4,22 @@
 // The sums of the hot loop (source/kernel.cu:484-631 standard, :368-477 generalized) are
 // recast as small complex matrix products. Within one work unit (object o, frequencies
 // k = kT + p + 128 m, p < 128, m < NM) the phase of observation j is
-//   theta_jk = alpha_jp + m beta_j,  alpha_jp = (fmin + (kT + p) df) t_j,  beta_j = 128 df t_j,
-// so with A[p][j] = v_j exp(i alpha_jp) and B[m][j] = exp(i m beta_j)
+//   theta_jk = alpha_jp + gamma_jm,  alpha_jp = a_j + p b_j,  gamma_jm = (kT + 128 m) b_j
+// (a_j, b_j: the exact 64-bit fixed-point phase of ObsRec, a + k b mod 2^64 turns), so
+// with A[p][j] = v_j exp(i alpha_jp) and B[m][j] = exp(i gamma_jm)
 //   sum_j v_j exp(i theta_jk) = (A B^T)[p][m],
 // and the squared terms follow from the doubled angle, cos^2 = (1 + cos 2theta) / 2,
 // cos sin = sin 2theta / 2, with A2 = exp(2i alpha) (times v for the generalized variant)
-// and B2 = exp(2i m beta). Both angles come from the exact 64-bit fixed-point phases of
-// ObsRec (a + k b mod 2^64 turns).
+// and B2 = exp(2i gamma). A does not depend on the frequency tile: it is computed once per
+// batch into the operand table (agen_kernel) and bulk-copied into every stage, so the
+// kernel's producers compute only the NM x 16 entries of B per K-block.
 //
 // Each complex product is two real MMAs with N = 2 NM: [Re | Im] = Ar [Br | Bi]^T +
 // Ai [-Bi | Br]^T, the right factors being two overlapping row windows of
 // Z = [-Bi; Br; Bi]. FP32 accuracy on the FP16 tensor cores comes from the split
 // x = hi + lo (hi: x rounded to 11 significant bits, lo = x - hi rounded to FP16),
-// a b ~ ah bh + ah bl + al bh: every operand is a cosine or sine times a weight
-// scaled into [-1, 1] by a power of two per object (ObjInfo::tsc0/tsc1), so hi + lo
+// a b ~ ah bh + ah bl + al bh: every operand is a cosine or sine, times a weight scaled
+// into [-1, 1] by a power of two per object (ObjInfo::tsc0/tsc1) on the A side, so hi + lo
 // carries x to about 2^-24 (lo may be subnormal, whose absolute spacing is 2^-24).
 //
 // The tensor cores round their FP32 accumulations toward zero, which makes the error of
@@ -28,19 +30,14 @@
 // the powers from the running sums.
 //
 // One persistent CTA per SM, warp-specialized:
-//   warps 0-3, 15-18  fold and epilogue, two warps per TMEM lane quarter (warp w may
+//   warps 0-3, 10-13  fold and epilogue, two warps per TMEM lane quarter (warp w may
 //               access lanes 32 (w % 4) ..): power per frequency, periodogram store,
 //               per-object maximum;
 //   warp 4      TMEM allocation and the MMA issuer (one thread);
-//   warp 5      record loader (one thread): bulk copies of 16 ObsRec per K-block into a
-//               shared-memory ring;
-//   warp 14     Z loader (one thread): bulk copies of the K-block's right operand from
-//               the Z table (zgen_kernel, once per batch: it does not depend on the
-//               frequency tile) into the operand stage;
-//   warps 6-13  producers: the split FP16 left operands of one K-block (16 observations) per
-//               stage of a shared-memory ring, K-major without swizzle. A thread computes
-//               A rows p and p + kTensorRowStep, the second by rotating the first with
-//               the record's (cd, sd), so half the A entries need no SFU sine/cosine.
+//   warp 5      operand loader (one thread): bulk copies of the K-block's A matrices and
+//               frequency steps b from the operand table into the stage;
+//   warps 6-9   producers: the split FP16 Z matrix of the stage's K-block, K-major
+//               without swizzle, one sine/cosine per entry.
 // All hand-offs use mbarriers. Every wait is bounded: on a timeout the kernel records an
 // error in MixedArgs::status, lets its issued MMAs drain, frees its TMEM and returns.
 #include <cuda_fp16.h>
@@ -57,13 +54,15 @@ namespace {
 constexpr int kTP = 128;        // fine frequency offsets p: A rows, TMEM lanes
 constexpr int kTK = 16;         // observations per K-block (the FP16 MMA depth)
 constexpr int kPassKB = 4;      // K-blocks accumulated in TMEM before an FP32 fold
-constexpr int kRecSlots = 8;    // record ring depth (K-blocks)
-constexpr int kRecSlotBytes = kTK * 32;
-constexpr int kThreads = 608;   // 19 warps
-constexpr int kZLoaderWarp = 14;
+// 14 warps: at most 4 per SM sub-partition, so up to 128 registers per thread
+constexpr int kThreads = 448;
+constexpr int kLoaderWarp = 5;
 constexpr int kProducerWarp0 = 6;
-constexpr int kProducerThreads = 256;
-constexpr int kEpilogueThreads = 256;  // warps 0-3 and 15-18
+constexpr int kProducerWarps = 4;
+constexpr int kProducerThreads = 32 * kProducerWarps;
+constexpr int kEpilogueWarp1 = kProducerWarp0 + kProducerWarps;  // second group: 10-13
+constexpr int kEpilogueThreads = 256;  // warps 0-3 and 10-13
+constexpr int kBBytes = kTK * 8;       // the K-block's frequency steps b (64-bit each)
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kBufCols = 128;   // TMEM columns of one partial buffer (two of them)
 constexpr uint32_t kRun0Col = 256;   // running sums of phase 0 (exp(i theta) sums)
@@ -81,14 +80,25 @@ struct TGeo {
     static constexpr int A_BYTES = kTP * kTK * 2;  // one 128 x 16 FP16 matrix
     static constexpr int Z_ROWS = 3 * NM;
     static constexpr int Z_BYTES = Z_ROWS * kTK * 2;
-    // stage: A matrices (group g, re/im, hi/lo) then the Z matrix (hi, lo)
+    // stage: A matrices (group g, re/im, hi/lo), the Z matrix (hi, lo), the steps b
     static constexpr int Z_OFF = NAG0 * 4 * A_BYTES;
-    static constexpr int STAGE = ((Z_OFF + 2 * Z_BYTES) + 1023) / 1024 * 1024;
+    static constexpr int B_OFF = Z_OFF + 2 * Z_BYTES;
+    static constexpr int STAGE = (B_OFF + kBBytes + 1023) / 1024 * 1024;
     static constexpr int STAGES = GEN ? 5 : 6;
     static constexpr int TILE = kTP * NM;          // frequencies per unit
+    // operand table, per K-block: phase 0 (NAG0 groups) then phase 1 (one group), each
+    // its A matrices followed by the 16 steps b
+    static constexpr int T0_BYTES = Z_OFF + kBBytes;
+    static constexpr int T1_BYTES = 4 * A_BYTES + kBBytes;
+    static constexpr int KB_BYTES = T0_BYTES + T1_BYTES;
+    // producers: one row m and JPT consecutive observations per thread; the K-block's 16
+    // observations in JS slices, a warp's lanes over 8 rows x JS slices x (4 / JS) row groups
+    static constexpr int JPT = NM / 8;
+    static constexpr int JS = kTK / JPT;
     static_assert(W0 <= (int)kBufCols && W1 <= (int)kBufCols, "partial buffer too narrow");
     static_assert(kRun1Col + W1 <= kTmemCols && kRun0Col + W0 <= kRun1Col, "TMEM layout");
-    static_assert(NM % 32 == 0, "Z rows in groups of 32 per producer thread");
+    static_assert(NM % 32 == 0 && (JPT == 4 || JPT == 8), "producer mapping");
+    static_assert(NM * kTK == kProducerThreads * JPT, "one Z entry per producer and observation");
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -277,7 +287,7 @@ __device__ __forceinline__ void turn_sincos(uint32_t hi, float &s, float &c) {
 }
 
 struct UnitInfo {
-    uint32_t o, tile, n, nkb;
+    uint32_t o, tile, n, nkb, kb0;
     uint64_t row0;
 };
 
@@ -287,6 +297,7 @@ __device__ __forceinline__ UnitInfo unit_info_of(const MixedArgs &a, uint32_t u,
     w.tile = u % a.n_tiles;
     w.row0 = a.objs[o].row0;
     w.n = a.objs[o].n;
+    w.kb0 = a.objs[o].kb0;
     w.nkb = (w.n + kTK - 1) / kTK;
     return w;
 }
@@ -320,9 +331,9 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *ring = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    unsigned char *recring = ring + (size_t)S * G::STAGE;  // kRecSlots x 512 bytes
-    __shared__ __align__(8) uint64_t full_bar[S], empty_bar[S];
-    __shared__ __align__(8) uint64_t rfull_bar[kRecSlots], rempty_bar[kRecSlots];
+    // afull: the stage's A matrices and steps b have landed (loader's bytes);
+    // full: its Z matrix is written (producers); empty: its MMAs have completed
+    __shared__ __align__(8) uint64_t afull_bar[S], full_bar[S], empty_bar[S];
     __shared__ __align__(8) uint64_t pfull_bar[2], pempty_bar[2], drain_bar;
     __shared__ uint32_t s_tmem;
     __shared__ volatile uint32_t s_abort;
@@ -332,12 +343,9 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
 
     if (tid == 0) {
         for (int s = 0; s < S; ++s) {
-            mbar_init(&full_bar[s], kProducerThreads + 1);  // + the Z loader's bytes
+            mbar_init(&afull_bar[s], 1);
+            mbar_init(&full_bar[s], kProducerThreads);
             mbar_init(&empty_bar[s], 1);
-        }
-        for (int r = 0; r < kRecSlots; ++r) {
-            mbar_init(&rfull_bar[r], 1);
-            mbar_init(&rempty_bar[r], kProducerThreads);
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(&pfull_bar[b], 1);
@@ -362,145 +370,103 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
     // Every role walks the same sequence: units b, b + grid, ...; in each unit phase 0
     // (exp(i theta) sums) then phase 1 (exp(2i theta) sums), each over the unit's nkb
     // K-blocks, cut into passes of kPassKB K-blocks.
-    if (warp >= kProducerWarp0 && warp < kZLoaderWarp) {
+    if (warp >= kProducerWarp0 && warp < kEpilogueWarp1) {
         // ---------------- producers ----------------
-        const uint32_t pw = (uint32_t)(warp - kProducerWarp0);  // 0..7
-        // A: rows p and p + kTensorRowStep (the second by the record's rotation), the
-        // four observations 8h + 4qd .. of the K-block. One 8-byte store per row and
-        // matrix; a half-warp writes 8 rows x 16 bytes = 128 contiguous bytes.
-        const uint32_t qd = (lane >> 3) & 1u, h = lane >> 4;
-        const uint32_t p = 16u * pw + (lane & 7u);
-        const uint32_t ja = 8u * h + 4u * qd;
-        const uint32_t offa0 = kmaj_off(p, ja), offa1 = kmaj_off(p + kTensorRowStep, ja);
+        // Z entry (m, j): B = exp(i (kT + 128 m) b_j) (phase 0) or its square (phase 1).
+        // A thread owns row m and the JPT observations j0.. of the K-block: one 2 JPT-byte
+        // store per row kind (-Bi, Br, Bi) and half (hi, lo). The lanes of a quarter-warp
+        // own 8 consecutive rows of one core matrix, so the stores have no bank conflicts.
+        constexpr uint32_t JPT = (uint32_t)G::JPT, JS = (uint32_t)G::JS;
+        const uint32_t pw = (uint32_t)(warp - kProducerWarp0);
+        const uint32_t sl_ = ((uint32_t)lane >> 3) % JS, rg = ((uint32_t)lane >> 3) / JS;
+        const uint32_t m = 8u * (pw * (4u / JS) + rg) + ((uint32_t)lane & 7u);
+        const uint32_t j0 = JPT * sl_;
+        // rows m (-Bi), NM + m (Br), 2 NM + m (Bi) of the hi matrix; lo is Z_BYTES further
+        const uint32_t zo = (uint32_t)G::Z_OFF + kmaj_off(m, j0);
+        constexpr uint32_t kRowNM = (uint32_t)G::NM * 32u;  // kmaj_off(r + NM) - kmaj_off(r)
         uint32_t g = 0;
         UnitWalk walk(a, units);
         for (uint32_t u = blockIdx.x; u < units && !s_abort; u += gridDim.x) {
             const UnitInfo w = walk.next(a, u, units);
-            const uint32_t kT = w.tile * (uint32_t)G::TILE;
-            const ObjInfo &ob = a.objs[w.o];
-            const float sc0 = ob.tsc0, sc1 = ob.tsc1;
+            const uint32_t k = w.tile * (uint32_t)G::TILE + 128u * m;
             for (uint32_t ks = 0; ks < 2u * w.nkb; ++ks, ++g) {
                 const bool ph1 = ks >= w.nkb;
-                const uint32_t kb = ph1 ? ks - w.nkb : ks;
-                const uint32_t r = g % kRecSlots, ur = g / kRecSlots;
                 const uint32_t s = g % S, us = g / S;
-                if (!mbar_wait(&rfull_bar[r], ur & 1u, &s_abort, a.status)) break;
-                const unsigned char *rs = recring + (size_t)r * kRecSlotBytes;
-                const uint32_t cnt = min((uint32_t)kTK, w.n - kb * kTK);
-                uint4 ra[4];
-                float4 va[4];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const uint32_t jj = min(ja + (uint32_t)q, cnt - 1u);
-                    ra[q] = *reinterpret_cast<const uint4 *>(rs + 32u * jj);
-                    va[q] = *reinterpret_cast<const float4 *>(rs + 32u * jj + 16u);
-                }
-                // the slot's next bulk copy is an async-proxy write: order these
-                // generic-proxy reads before it (write-after-read across proxies)
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                mbar_arrive(&rempty_bar[r]);
-                if (!mbar_wait(&empty_bar[s], (us & 1u) ^ 1u, &s_abort, a.status)) break;
+                if (!mbar_wait(&afull_bar[s], us & 1u, &s_abort, a.status)) break;
                 unsigned char *st = ring + (size_t)s * G::STAGE;
-                // ---- A operands ----
-                {
-                    const uint32_t ka = kT + p;
-                    // values [row][quantity][observation]; observations past the object's
-                    // end (clamped records, finite values) are cancelled by zero Z entries
-                    float x0[2][4], x1[2][4], x2[2][4], x3[2][4];
+                // packed FP16 pairs (j, j + 1) of cos and sin, hi and lo
+                uint32_t pch[JPT / 2], pcl[JPT / 2], psh[JPT / 2], psl[JPT / 2];
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const uint64_t ph =
-                            (uint64_t)ka * ra[q].z + (((uint64_t)ra[q].y << 32) | ra[q].x);
-                        const uint32_t hi = (uint32_t)(ph >> 32) + ka * ra[q].w;
-                        float sn[2], cs[2];
-                        turn_sincos(hi, sn[0], cs[0]);
-                        cs[1] = fmaf(cs[0], va[q].z, -sn[0] * va[q].w);  // rotate by s grid points
-                        sn[1] = fmaf(sn[0], va[q].z, cs[0] * va[q].w);
-                        const float v0 = va[q].x * sc0;
-                        const float v1 = va[q].y * sc1;
+                for (uint32_t h = 0; h < JPT / 2; ++h) {
+                    const uint4 bq =
+                        *reinterpret_cast<const uint4 *>(st + G::B_OFF + 8u * (j0 + 2u * h));
+                    const uint32_t bl[2] = {bq.x, bq.z}, bh[2] = {bq.y, bq.w};
+                    float ch[2], cl[2], sh[2], sl[2];
 #pragma unroll
-                        for (int rr = 0; rr < 2; ++rr) {
-                            if (!ph1) {
-                                x0[rr][q] = v0 * cs[rr];
-                                x1[rr][q] = v0 * sn[rr];
-                                if (GEN) {
-                                    x2[rr][q] = v1 * cs[rr];
-                                    x3[rr][q] = v1 * sn[rr];
-                                }
-                            } else {
-                                const float c2 = fmaf(cs[rr], cs[rr], -sn[rr] * sn[rr]);
-                                const float s2 = 2.0f * cs[rr] * sn[rr];
-                                // doubled angle, weighted for the generalized variant
-                                x0[rr][q] = GEN ? v0 * c2 : c2;
-                                x1[rr][q] = GEN ? v0 * s2 : s2;
-                            }
+                    for (int q = 0; q < 2; ++q) {
+                        // hi 32 bits of k b mod 2^64: (k b_lo) >> 32 plus k b_hi
+                        const uint32_t t32 = __umulhi(k, bl[q]) + k * bh[q];
+                        float sn, cs;
+                        turn_sincos(t32, sn, cs);
+                        if (ph1) {
+                            const float c2 = fmaf(cs, cs, -sn * sn);
+                            sn = 2.0f * cs * sn;
+                            cs = c2;
                         }
+                        vsplit(cs, ch[q], cl[q]);
+                        vsplit(sn, sh[q], sl[q]);
                     }
-                    auto put4 = [&](int mat, int rr, const float (&x)[2][4]) {
-                        float hi[4], lo[4];
-#pragma unroll
-                        for (int q = 0; q < 4; ++q) vsplit(x[rr][q], hi[q], lo[q]);
-                        unsigned char *base = st + (size_t)mat * G::A_BYTES + (rr ? offa1 : offa0);
-                        *reinterpret_cast<uint2 *>(base) =
-                            make_uint2(pack_h2(hi[0], hi[1]), pack_h2(hi[2], hi[3]));
-                        *reinterpret_cast<uint2 *>(base + G::A_BYTES) =
-                            make_uint2(pack_h2(lo[0], lo[1]), pack_h2(lo[2], lo[3]));
-                    };
-                    // matrix order: group g at 4g: re hi, re lo, im hi, im lo
-#pragma unroll
-                    for (int rr = 0; rr < 2; ++rr) {
-                        put4(0, rr, x0);
-                        put4(2, rr, x1);
-                        if (GEN && !ph1) {
-                            put4(4, rr, x2);
-                            put4(6, rr, x3);
-                        }
-                    }
+                    pch[h] = pack_h2(ch[0], ch[1]);
+                    pcl[h] = pack_h2(cl[0], cl[1]);
+                    psh[h] = pack_h2(sh[0], sh[1]);
+                    psl[h] = pack_h2(sl[0], sl[1]);
                 }
+                // -x = (-hi) + (-lo) exactly: the sign bits of both FP16 halves flipped
+                uint32_t nsh[JPT / 2], nsl[JPT / 2];
+#pragma unroll
+                for (uint32_t h = 0; h < JPT / 2; ++h) {
+                    nsh[h] = psh[h] ^ 0x80008000u;
+                    nsl[h] = psl[h] ^ 0x80008000u;
+                }
+                unsigned char *zh = st + zo;
+                auto put = [&](unsigned char *dst, const uint32_t (&v)[JPT / 2]) {
+                    if constexpr (JPT == 8)
+                        *reinterpret_cast<uint4 *>(dst) = make_uint4(v[0], v[1], v[2], v[3]);
+                    else
+                        *reinterpret_cast<uint2 *>(dst) = make_uint2(v[0], v[1]);
+                };
+                put(zh, nsh);
+                put(zh + G::Z_BYTES, nsl);
+                put(zh + kRowNM, pch);
+                put(zh + kRowNM + G::Z_BYTES, pcl);
+                put(zh + 2u * kRowNM, psh);
+                put(zh + 2u * kRowNM + G::Z_BYTES, psl);
+                // generic-proxy stores -> the MMA's async-proxy reads; the same fence orders
+                // this thread's reads of the steps b before the stage's next bulk copy
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 mbar_arrive(&full_bar[s]);
             }
         }
-    } else if (warp == kZLoaderWarp) {
-        // ---------------- Z loader: the unit's right operands from the Z table ----------------
+    } else if (warp == kLoaderWarp) {
+        // ---------------- operand loader ----------------
         if (lane == 0) {
-            const unsigned char *zt = static_cast<const unsigned char *>(a.ztab);
+            const unsigned char *tab = static_cast<const unsigned char *>(a.optab);
             uint32_t g = 0;
             UnitWalk walk(a, units);
             for (uint32_t u = blockIdx.x; u < units && !s_abort; u += gridDim.x) {
                 const UnitInfo w = walk.next(a, u, units);
-                const uint32_t kb0 = a.objs[w.o].kb0;
                 for (uint32_t ks = 0; ks < 2u * w.nkb; ++ks, ++g) {
                     const uint32_t ph = ks >= w.nkb ? 1u : 0u;
                     const uint32_t kb = ph ? ks - w.nkb : ks;
                     const uint32_t s = g % S, us = g / S;
                     if (!mbar_wait(&empty_bar[s], (us & 1u) ^ 1u, &s_abort, a.status)) break;
-                    mbar_expect_tx(&full_bar[s], 2u * G::Z_BYTES);
-                    bulk_copy_g2s(ring + (size_t)s * G::STAGE + G::Z_OFF,
-                                  zt + ((uint64_t)(kb0 + kb) * 2u + ph) * 2u * G::Z_BYTES,
-                                  2u * G::Z_BYTES, &full_bar[s]);
-                }
-            }
-        }
-        __syncwarp();
-    } else if (warp == 5) {
-        // ---------------- record loader ----------------
-        if (lane == 0) {
-            const ObsRec *rec = static_cast<const ObsRec *>(a.rec);
-            uint32_t g = 0;
-            UnitWalk walk(a, units);
-            for (uint32_t u = blockIdx.x; u < units && !s_abort; u += gridDim.x) {
-                const UnitInfo w = walk.next(a, u, units);
-                for (uint32_t ks = 0; ks < 2u * w.nkb; ++ks, ++g) {
-                    const uint32_t kb = ks >= w.nkb ? ks - w.nkb : ks;
-                    const uint32_t r = g % kRecSlots, ur = g / kRecSlots;
-                    if (!mbar_wait(&rempty_bar[r], (ur & 1u) ^ 1u, &s_abort, a.status)) break;
-                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    const uint32_t cnt = min((uint32_t)kTK, w.n - kb * kTK);
-                    const uint32_t bytes = cnt * 32u;
-                    mbar_expect_tx(&rfull_bar[r], bytes);
-                    bulk_copy_g2s(recring + (size_t)r * kRecSlotBytes, rec + w.row0 + (uint64_t)kb * kTK,
-                                  bytes, &rfull_bar[r]);
+                    const uint32_t abytes = ph ? 4u * G::A_BYTES : (uint32_t)G::Z_OFF;
+                    const unsigned char *src = tab + (uint64_t)(w.kb0 + kb) * G::KB_BYTES +
+                                               (ph ? (uint32_t)G::T0_BYTES : 0u);
+                    unsigned char *st = ring + (size_t)s * G::STAGE;
+                    mbar_expect_tx(&afull_bar[s], abytes + (uint32_t)kBBytes);
+                    bulk_copy_g2s(st, src, abytes, &afull_bar[s]);
+                    bulk_copy_g2s(st + G::B_OFF, src + abytes, (uint32_t)kBBytes, &afull_bar[s]);
                 }
             }
         }
@@ -566,12 +532,12 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
         }
         __syncwarp();
     } else {
-        // ---------------- fold and epilogue (warps 0-3 and 15-18) ----------------
+        // ---------------- fold and epilogue (warps 0-3 and 10-13) ----------------
         // warp w may access TMEM lanes 32 (w % 4) ..; the two warps of a lane quarter split
         // the coarse steps: warp half eh owns m in [eh NM/2, (eh+1) NM/2), i.e. the same
         // half of every NM-column quantity block, in the folds and in the power pass, so a
         // warp only ever reads running sums it wrote itself
-        const uint32_t eq = (uint32_t)warp & 3u, eh = warp >= 15 ? 1u : 0u;
+        const uint32_t eq = (uint32_t)warp & 3u, eh = warp >= kEpilogueWarp1 ? 1u : 0u;
         const uint32_t pl = eq * 32u + (uint32_t)lane;
         const uint32_t lane_base = (eq * 32u) << 16;
         const uint32_t run1 = tmem + lane_base + kRun0Col, run2 = tmem + lane_base + kRun1Col;
@@ -665,9 +631,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                 for (int k = 0; k < NQ; ++k)
 #pragma unroll
                     for (int i = 0; i < 8; ++i) q[k][i] = __uint_as_float(x[k][i]);
-                if (PREFETCH && m0 + 8 < mend) load_chunk(m0 + 8);
-#pragma unroll
-                for (int i = 0; i < 8; ++i) {
+                auto power_at = [&](int i) {
                     const uint32_t k = kT + pl + (uint32_t)kTP * (uint32_t)(m0 + i);
                     float P;
                     if (GEN) {
@@ -686,7 +650,13 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                         if (a.pgram) store_out<OutT>(a.pgram, out0 + k, P);
                         if (P > bp) { bp = P; bk = k; }
                     }
-                }
+                };
+#pragma unroll
+                for (int i = 0; i < 4; ++i) power_at(i);
+                // the next chunk's load goes out once half of this chunk's values are dead
+                if (PREFETCH && m0 + 8 < mend) load_chunk(m0 + 8);
+#pragma unroll
+                for (int i = 4; i < 8; ++i) power_at(i);
             }
             if (a.best_key) {
 #pragma unroll
@@ -713,15 +683,17 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
     }
 }
 
-// The Z table: one CTA per (K-block, phase) builds the two Z matrices (hi, lo) of
-// Z = [-Bi; Br; Bi], B[m][j] = exp(i m beta_j) (phase 0) or exp(2i m beta_j) (phase 1), in
-// shared memory with the layout the tensor kernel stages, and copies them out coalesced.
-// Observations past the object's end get zero entries, which cancel the A side's entries
-// of the clamped records in every product.
+// The operand table: one CTA per (K-block, phase) builds the K-block's A matrices for
+// p < 128, split FP16 (group g, re / im, hi / lo) in the layout the tensor kernel stages,
+// followed by the 16 observations' frequency steps b, and copies them out coalesced.
+//   phase 0: v0 tsc0 exp(i alpha) (and v1 tsc1 exp(i alpha), generalized)
+//   phase 1: exp(2i alpha) (standard) or v0 tsc0 exp(2i alpha) (generalized)
+// with alpha = a + p b in 64-bit fixed point. Observations past the object's end get zero
+// A entries (and b = 0), so they add nothing to any product.
 template <bool GEN>
-__global__ void __launch_bounds__(256) zgen_kernel(MixedArgs a, uint32_t total_kb) {
+__global__ void __launch_bounds__(256) agen_kernel(MixedArgs a, uint32_t total_kb) {
     using G = TGeo<GEN>;
-    __shared__ __align__(16) unsigned char zs[2 * G::Z_BYTES];
+    __shared__ __align__(16) unsigned char ts[G::T0_BYTES];
     const uint32_t kbg = blockIdx.x >> 1, ph = blockIdx.x & 1u;
     if (kbg >= total_kb) return;
     // the object of this K-block: the last o with kb0 <= kbg
@@ -734,47 +706,64 @@ __global__ void __launch_bounds__(256) zgen_kernel(MixedArgs a, uint32_t total_k
     const uint32_t kb = kbg - ob.kb0;
     const uint32_t cnt = min((uint32_t)kTK, ob.n - kb * kTK);
     const ObsRec *rec = static_cast<const ObsRec *>(a.rec) + ob.row0 + (uint64_t)kb * kTK;
-    for (uint32_t e = threadIdx.x; e < (uint32_t)G::NM * (kTK / 2); e += blockDim.x) {
-        const uint32_t m = e / (kTK / 2), j0 = 2u * (e % (kTK / 2));
-        const uint32_t k128 = 128u * m;
-        float h[2][2], l[2][2];  // [cos / sin][observation]
+    const float sc0 = ob.tsc0, sc1 = ob.tsc1;
+    const uint32_t nag = ph ? 1u : (uint32_t)G::NAG0;
+    const uint32_t abytes = nag * 4u * G::A_BYTES;
+    for (uint32_t e = threadIdx.x; e < (uint32_t)kTP * (kTK / 4); e += blockDim.x) {
+        const uint32_t p = e >> 2, j0 = 4u * (e & 3u);
+        float x[2][2][4];  // [group][re / im][observation]
 #pragma unroll
-        for (int q = 0; q < 2; ++q) {
+        for (int q = 0; q < 4; ++q) {
             const uint32_t j = j0 + (uint32_t)q;
             const ObsRec &r = rec[min(j, cnt - 1u)];
-            const uint64_t pz = (uint64_t)k128 * r.b_lo;
-            const uint32_t t32 = (uint32_t)(pz >> 32) + k128 * r.b_hi;
+            const uint64_t pa = (uint64_t)p * r.b_lo + (((uint64_t)r.a_hi << 32) | r.a_lo);
+            const uint32_t t32 = (uint32_t)(pa >> 32) + p * r.b_hi;
             float sn, cs;
             turn_sincos(t32, sn, cs);
-            if (ph) {
-                const float c2 = fmaf(cs, cs, -sn * sn);
-                sn = 2.0f * cs * sn;
-                cs = c2;
-            }
             const float mk = j < cnt ? 1.0f : 0.0f;
-            vsplit(cs * mk, h[0][q], l[0][q]);
-            vsplit(sn * mk, h[1][q], l[1][q]);
+            if (ph == 0) {
+                const float v0 = r.v0 * sc0 * mk, v1 = r.v1 * sc1 * mk;
+                x[0][0][q] = v0 * cs;
+                x[0][1][q] = v0 * sn;
+                x[1][0][q] = v1 * cs;
+                x[1][1][q] = v1 * sn;
+            } else {
+                const float wt = (GEN ? r.v0 * sc0 : 1.0f) * mk;
+                x[0][0][q] = wt * fmaf(cs, cs, -sn * sn);
+                x[0][1][q] = wt * (2.0f * cs * sn);
+                x[1][0][q] = 0.0f;
+                x[1][1][q] = 0.0f;
+            }
         }
-        // -x = (-hi) + (-lo) exactly; hi matrix then lo matrix
-        auto putz = [&](uint32_t row, int v, float sg) {
-            unsigned char *base = zs + kmaj_off(row, j0);
-            *reinterpret_cast<uint32_t *>(base) = pack_h2(sg * h[v][0], sg * h[v][1]);
-            *reinterpret_cast<uint32_t *>(base + G::Z_BYTES) = pack_h2(sg * l[v][0], sg * l[v][1]);
-        };
-        putz(m, 1, -1.0f);
-        putz(G::NM + m, 0, 1.0f);
-        putz(2 * G::NM + m, 1, 1.0f);
+        for (uint32_t gi = 0; gi < nag; ++gi) {
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                float h4[4], l4[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) vsplit(x[gi][c][q], h4[q], l4[q]);
+                unsigned char *base = ts + (4u * gi + 2u * (uint32_t)c) * G::A_BYTES + kmaj_off(p, j0);
+                *reinterpret_cast<uint2 *>(base) = make_uint2(pack_h2(h4[0], h4[1]), pack_h2(h4[2], h4[3]));
+                *reinterpret_cast<uint2 *>(base + G::A_BYTES) =
+                    make_uint2(pack_h2(l4[0], l4[1]), pack_h2(l4[2], l4[3]));
+            }
+        }
+    }
+    if (threadIdx.x < (uint32_t)kTK) {
+        const uint32_t j = threadIdx.x;
+        uint2 b = make_uint2(0u, 0u);
+        if (j < cnt) b = make_uint2(rec[j].b_lo, rec[j].b_hi);
+        *reinterpret_cast<uint2 *>(ts + abytes + 8u * j) = b;
     }
     __syncthreads();
-    uint4 *dst = reinterpret_cast<uint4 *>(const_cast<void *>(a.ztab)) +
-                 ((uint64_t)kbg * 2u + ph) * (2u * G::Z_BYTES / 16u);
-    const uint4 *src = reinterpret_cast<const uint4 *>(zs);
-    for (uint32_t i = threadIdx.x; i < 2u * G::Z_BYTES / 16u; i += blockDim.x) dst[i] = src[i];
+    uint4 *dst = reinterpret_cast<uint4 *>(static_cast<unsigned char *>(const_cast<void *>(a.optab)) +
+                                           (uint64_t)kbg * G::KB_BYTES + (ph ? G::T0_BYTES : 0));
+    const uint4 *src = reinterpret_cast<const uint4 *>(ts);
+    for (uint32_t i = threadIdx.x; i < (abytes + (uint32_t)kBBytes) / 16u; i += blockDim.x) dst[i] = src[i];
 }
 
 template <bool GEN>
 size_t tensor_smem() {
-    return (size_t)TGeo<GEN>::STAGES * TGeo<GEN>::STAGE + (size_t)kRecSlots * kRecSlotBytes + 1024;
+    return (size_t)TGeo<GEN>::STAGES * TGeo<GEN>::STAGE + 1024;
 }
 
 template <bool GEN, typename OutT>
@@ -795,19 +784,18 @@ uint32_t tensor_tile_freqs(int variant) {
 
 size_t tensor_smem_bytes(int variant) { return variant ? tensor_smem<true>() : tensor_smem<false>(); }
 
-size_t tensor_ztab_bytes(int variant, uint64_t total_kb) {
-    return (size_t)total_kb * 2u * 2u *
-           (size_t)(variant ? TGeo<true>::Z_BYTES : TGeo<false>::Z_BYTES);
+size_t tensor_optab_bytes(int variant, uint64_t total_kb) {
+    return (size_t)total_kb * (size_t)(variant ? TGeo<true>::KB_BYTES : TGeo<false>::KB_BYTES);
 }
 
-cudaError_t launch_tensor_ztab(int variant, const MixedArgs &a, uint64_t total_kb, cudaStream_t st) {
+cudaError_t launch_tensor_optab(int variant, const MixedArgs &a, uint64_t total_kb, cudaStream_t st) {
     if (total_kb == 0) return cudaSuccess;
     const uint64_t blocks = total_kb * 2u;
     if (blocks > 0x7fffffffull) return cudaErrorInvalidValue;
     if (variant == 0)
-        zgen_kernel<false><<<(unsigned)blocks, 256, 0, st>>>(a, (uint32_t)total_kb);
+        agen_kernel<false><<<(unsigned)blocks, 256, 0, st>>>(a, (uint32_t)total_kb);
     else
-        zgen_kernel<true><<<(unsigned)blocks, 256, 0, st>>>(a, (uint32_t)total_kb);
+        agen_kernel<true><<<(unsigned)blocks, 256, 0, st>>>(a, (uint32_t)total_kb);
     return cudaGetLastError();
 }
 
