@@ -298,7 +298,8 @@ int enqueue_batch(Batch &b, Workspace &ws, cudaStream_t st, cudaEvent_t ev0, cud
         ++kernels;
         MixedArgs a{};
         a.rec = ws.rec.p;
-        a.optab = ws.optab.p;
+        a.steps = ws.optab.p;
+        a.optab = (const unsigned char *)ws.optab.p + b.total_kb * kTensorStepBytes;
         a.objs = d_objs;
         a.perm = (const uint32_t *)ws.perm.p;
         a.n_obj = b.n_obj;

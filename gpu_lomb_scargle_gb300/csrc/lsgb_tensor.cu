@@ -30,14 +30,16 @@
 // the powers from the running sums.
 //
 // One persistent CTA per SM, warp-specialized:
-//   warps 0-3, 10-13  fold and epilogue, two warps per TMEM lane quarter (warp w may
+//   warps 0-3 and the four after the producers: fold and epilogue, two warps per TMEM lane quarter (warp w may
 //               access lanes 32 (w % 4) ..): power per frequency, periodogram store,
 //               per-object maximum;
 //   warp 4      TMEM allocation and the MMA issuer (one thread);
-//   warp 5      operand loader (one thread): bulk copies of the K-block's A matrices and
-//               frequency steps b from the operand table into the stage;
-//   warps 6-9   producers: the split FP16 Z matrix of the stage's K-block, K-major
-//               without swizzle, one sine/cosine per entry.
+//   warp 5      operand loader (one thread): bulk copies of the K-block's A matrices from
+//               the operand table into the stage, and L2 prefetches of the table ahead;
+//   warps 6..   producers (kProducerWarps): the split FP16 Z matrix of the stage's K-block,
+//               K-major without swizzle, one sine/cosine per entry, from the K-block's
+//               frequency steps (read from global memory one stage ahead). They start as
+//               soon as the stage is free, in parallel with its bulk copy.
 // All hand-offs use mbarriers. Every wait is bounded: on a timeout the kernel records an
 // error in MixedArgs::status, lets its issued MMAs drain, frees its TMEM and returns.
 #include <cuda_fp16.h>
@@ -54,15 +56,19 @@ namespace {
 constexpr int kTP = 128;        // fine frequency offsets p: A rows, TMEM lanes
 constexpr int kTK = 16;         // observations per K-block (the FP16 MMA depth)
 constexpr int kPassKB = 4;      // K-blocks accumulated in TMEM before an FP32 fold
-// 14 warps: at most 4 per SM sub-partition, so up to 128 registers per thread
-constexpr int kThreads = 448;
 constexpr int kLoaderWarp = 5;
 constexpr int kProducerWarp0 = 6;
-constexpr int kProducerWarps = 4;
+#ifndef LSGB_TENSOR_PRODUCER_WARPS
+#define LSGB_TENSOR_PRODUCER_WARPS 4
+#endif
+// 4 producer warps: 14 warps, at most 4 per SM sub-partition, so up to 128 registers per
+// thread; 8: 18 warps and 96 registers
+constexpr int kProducerWarps = LSGB_TENSOR_PRODUCER_WARPS;
 constexpr int kProducerThreads = 32 * kProducerWarps;
-constexpr int kEpilogueWarp1 = kProducerWarp0 + kProducerWarps;  // second group: 10-13
-constexpr int kEpilogueThreads = 256;  // warps 0-3 and 10-13
-constexpr int kBBytes = kTK * 8;       // the K-block's frequency steps b (64-bit each)
+constexpr int kEpilogueWarp1 = kProducerWarp0 + kProducerWarps;  // second epilogue group
+constexpr int kThreads = 32 * (kEpilogueWarp1 + 4);
+constexpr int kEpilogueThreads = 256;  // warps 0-3 and kEpilogueWarp1..+3
+constexpr uint32_t kPrefetchKB = 32;   // operand-table K-blocks prefetched into L2 ahead
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kBufCols = 128;   // TMEM columns of one partial buffer (two of them)
 constexpr uint32_t kRun0Col = 256;   // running sums of phase 0 (exp(i theta) sums)
@@ -80,24 +86,22 @@ struct TGeo {
     static constexpr int A_BYTES = kTP * kTK * 2;  // one 128 x 16 FP16 matrix
     static constexpr int Z_ROWS = 3 * NM;
     static constexpr int Z_BYTES = Z_ROWS * kTK * 2;
-    // stage: A matrices (group g, re/im, hi/lo), the Z matrix (hi, lo), the steps b
+    // stage: A matrices (group g, re/im, hi/lo), then the Z matrix (hi, lo)
     static constexpr int Z_OFF = NAG0 * 4 * A_BYTES;
-    static constexpr int B_OFF = Z_OFF + 2 * Z_BYTES;
-    static constexpr int STAGE = (B_OFF + kBBytes + 1023) / 1024 * 1024;
-    static constexpr int STAGES = GEN ? 5 : 6;
+    static constexpr int STAGE = (Z_OFF + 2 * Z_BYTES + 1023) / 1024 * 1024;
+    static constexpr int STAGES = GEN ? 5 : 7;
     static constexpr int TILE = kTP * NM;          // frequencies per unit
-    // operand table, per K-block: phase 0 (NAG0 groups) then phase 1 (one group), each
-    // its A matrices followed by the 16 steps b
-    static constexpr int T0_BYTES = Z_OFF + kBBytes;
-    static constexpr int T1_BYTES = 4 * A_BYTES + kBBytes;
+    // operand table, per K-block: the A matrices of phase 0 (NAG0 groups), then of phase 1
+    static constexpr int T0_BYTES = Z_OFF;
+    static constexpr int T1_BYTES = 4 * A_BYTES;
     static constexpr int KB_BYTES = T0_BYTES + T1_BYTES;
     // producers: one row m and JPT consecutive observations per thread; the K-block's 16
-    // observations in JS slices, a warp's lanes over 8 rows x JS slices x (4 / JS) row groups
-    static constexpr int JPT = NM / 8;
+    // observations in JS slices
+    static constexpr int JPT = NM * kTK / kProducerThreads;
     static constexpr int JS = kTK / JPT;
     static_assert(W0 <= (int)kBufCols && W1 <= (int)kBufCols, "partial buffer too narrow");
     static_assert(kRun1Col + W1 <= kTmemCols && kRun0Col + W0 <= kRun1Col, "TMEM layout");
-    static_assert(NM % 32 == 0 && (JPT == 4 || JPT == 8), "producer mapping");
+    static_assert(NM % 32 == 0 && (JPT == 2 || JPT == 4 || JPT == 8), "producer mapping");
     static_assert(NM * kTK == kProducerThreads * JPT, "one Z entry per producer and observation");
 };
 
@@ -182,6 +186,12 @@ __device__ __noinline__ bool mbar_wait_slow(uint64_t *b, uint32_t parity,
 __device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, volatile uint32_t *abort,
                                           uint32_t *status) {
     return mbar_test(b, parity) || mbar_wait_slow(b, parity, abort, status);
+}
+
+__device__ __forceinline__ void bulk_prefetch_l2(const void *src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(__cvta_generic_to_global(src)),
+                 "r"(bytes)
+                 : "memory");
 }
 
 __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes,
@@ -331,9 +341,10 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *ring = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    // afull: the stage's A matrices and steps b have landed (loader's bytes);
-    // full: its Z matrix is written (producers); empty: its MMAs have completed
-    __shared__ __align__(8) uint64_t afull_bar[S], full_bar[S], empty_bar[S];
+    // full: the stage's A matrices have landed (the loader's arrival and bytes) and its Z
+    // matrix is written (the producers' arrivals); empty: its MMAs have completed (the
+    // loader and the producers wait for it)
+    __shared__ __align__(8) uint64_t full_bar[S], empty_bar[S];
     __shared__ __align__(8) uint64_t pfull_bar[2], pempty_bar[2], drain_bar;
     __shared__ uint32_t s_tmem;
     __shared__ volatile uint32_t s_abort;
@@ -343,8 +354,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
 
     if (tid == 0) {
         for (int s = 0; s < S; ++s) {
-            mbar_init(&afull_bar[s], 1);
-            mbar_init(&full_bar[s], kProducerThreads);
+            mbar_init(&full_bar[s], kProducerThreads + 1);
             mbar_init(&empty_bar[s], 1);
         }
         for (int b = 0; b < 2; ++b) {
@@ -377,30 +387,44 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
         // store per row kind (-Bi, Br, Bi) and half (hi, lo). The lanes of a quarter-warp
         // own 8 consecutive rows of one core matrix, so the stores have no bank conflicts.
         constexpr uint32_t JPT = (uint32_t)G::JPT, JS = (uint32_t)G::JS;
-        const uint32_t pw = (uint32_t)(warp - kProducerWarp0);
-        const uint32_t sl_ = ((uint32_t)lane >> 3) % JS, rg = ((uint32_t)lane >> 3) / JS;
-        const uint32_t m = 8u * (pw * (4u / JS) + rg) + ((uint32_t)lane & 7u);
-        const uint32_t j0 = JPT * sl_;
+        // quarter-warp c of the producers: observation slice c % JS, row group c / JS
+        const uint32_t c = ((uint32_t)lane >> 3) + 4u * (uint32_t)(warp - kProducerWarp0);
+        const uint32_t m = 8u * (c / JS) + ((uint32_t)lane & 7u);
+        const uint32_t j0 = JPT * (c % JS);
         // rows m (-Bi), NM + m (Br), 2 NM + m (Bi) of the hi matrix; lo is Z_BYTES further
         const uint32_t zo = (uint32_t)G::Z_OFF + kmaj_off(m, j0);
         constexpr uint32_t kRowNM = (uint32_t)G::NM * 32u;  // kmaj_off(r + NM) - kmaj_off(r)
         uint32_t g = 0;
         UnitWalk walk(a, units);
+        // the steps b of the next stage's K-block, loaded one stage ahead
+        const uint4 *steps = static_cast<const uint4 *>(a.steps);
+        uint4 nb[JPT / 2];
+        auto load_b = [&](uint32_t kbg) {
+#pragma unroll
+            for (uint32_t h = 0; h < JPT / 2; ++h) nb[h] = __ldg(steps + (kbg * kTK + j0) / 2u + h);
+        };
+        if (blockIdx.x < units) load_b(walk.nxt.kb0);
         for (uint32_t u = blockIdx.x; u < units && !s_abort; u += gridDim.x) {
             const UnitInfo w = walk.next(a, u, units);
             const uint32_t k = w.tile * (uint32_t)G::TILE + 128u * m;
             for (uint32_t ks = 0; ks < 2u * w.nkb; ++ks, ++g) {
                 const bool ph1 = ks >= w.nkb;
                 const uint32_t s = g % S, us = g / S;
-                if (!mbar_wait(&afull_bar[s], us & 1u, &s_abort, a.status)) break;
+                uint4 cb[JPT / 2];
+#pragma unroll
+                for (uint32_t h = 0; h < JPT / 2; ++h) cb[h] = nb[h];
+                const uint32_t ks1 = ks + 1u;
+                if (ks1 < 2u * w.nkb)
+                    load_b(w.kb0 + (ks1 < w.nkb ? ks1 : ks1 - w.nkb));
+                else if (u + gridDim.x < units)
+                    load_b(walk.nxt.kb0);
+                if (!mbar_wait(&empty_bar[s], (us & 1u) ^ 1u, &s_abort, a.status)) break;
                 unsigned char *st = ring + (size_t)s * G::STAGE;
                 // packed FP16 pairs (j, j + 1) of cos and sin, hi and lo
                 uint32_t pch[JPT / 2], pcl[JPT / 2], psh[JPT / 2], psl[JPT / 2];
 #pragma unroll
                 for (uint32_t h = 0; h < JPT / 2; ++h) {
-                    const uint4 bq =
-                        *reinterpret_cast<const uint4 *>(st + G::B_OFF + 8u * (j0 + 2u * h));
-                    const uint32_t bl[2] = {bq.x, bq.z}, bh[2] = {bq.y, bq.w};
+                    const uint32_t bl[2] = {cb[h].x, cb[h].z}, bh[2] = {cb[h].y, cb[h].w};
                     float ch[2], cl[2], sh[2], sl[2];
 #pragma unroll
                     for (int q = 0; q < 2; ++q) {
@@ -432,8 +456,10 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                 auto put = [&](unsigned char *dst, const uint32_t (&v)[JPT / 2]) {
                     if constexpr (JPT == 8)
                         *reinterpret_cast<uint4 *>(dst) = make_uint4(v[0], v[1], v[2], v[3]);
-                    else
+                    else if constexpr (JPT == 4)
                         *reinterpret_cast<uint2 *>(dst) = make_uint2(v[0], v[1]);
+                    else
+                        *reinterpret_cast<uint32_t *>(dst) = v[0];
                 };
                 put(zh, nsh);
                 put(zh + G::Z_BYTES, nsl);
@@ -441,8 +467,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                 put(zh + kRowNM + G::Z_BYTES, pcl);
                 put(zh + 2u * kRowNM, psh);
                 put(zh + 2u * kRowNM + G::Z_BYTES, psl);
-                // generic-proxy stores -> the MMA's async-proxy reads; the same fence orders
-                // this thread's reads of the steps b before the stage's next bulk copy
+                // generic-proxy stores -> the MMA's async-proxy reads
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 mbar_arrive(&full_bar[s]);
             }
@@ -453,20 +478,29 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             const unsigned char *tab = static_cast<const unsigned char *>(a.optab);
             uint32_t g = 0;
             UnitWalk walk(a, units);
+            if (blockIdx.x < units)
+                bulk_prefetch_l2(tab + (uint64_t)walk.nxt.kb0 * G::KB_BYTES,
+                                 min(walk.nxt.nkb, kPrefetchKB) * (uint32_t)G::KB_BYTES);
             for (uint32_t u = blockIdx.x; u < units && !s_abort; u += gridDim.x) {
                 const UnitInfo w = walk.next(a, u, units);
+                // L2: the next unit's first K-blocks now, this unit's further ones as the
+                // phase-0 pass reaches them
+                if (u + gridDim.x < units)
+                    bulk_prefetch_l2(tab + (uint64_t)walk.nxt.kb0 * G::KB_BYTES,
+                                     min(walk.nxt.nkb, kPrefetchKB) * (uint32_t)G::KB_BYTES);
                 for (uint32_t ks = 0; ks < 2u * w.nkb; ++ks, ++g) {
                     const uint32_t ph = ks >= w.nkb ? 1u : 0u;
                     const uint32_t kb = ph ? ks - w.nkb : ks;
                     const uint32_t s = g % S, us = g / S;
+                    if (!ph && kb + kPrefetchKB < w.nkb)
+                        bulk_prefetch_l2(tab + (uint64_t)(w.kb0 + kb + kPrefetchKB) * G::KB_BYTES,
+                                         (uint32_t)G::KB_BYTES);
                     if (!mbar_wait(&empty_bar[s], (us & 1u) ^ 1u, &s_abort, a.status)) break;
-                    const uint32_t abytes = ph ? 4u * G::A_BYTES : (uint32_t)G::Z_OFF;
+                    const uint32_t abytes = ph ? (uint32_t)G::T1_BYTES : (uint32_t)G::T0_BYTES;
                     const unsigned char *src = tab + (uint64_t)(w.kb0 + kb) * G::KB_BYTES +
                                                (ph ? (uint32_t)G::T0_BYTES : 0u);
-                    unsigned char *st = ring + (size_t)s * G::STAGE;
-                    mbar_expect_tx(&afull_bar[s], abytes + (uint32_t)kBBytes);
-                    bulk_copy_g2s(st, src, abytes, &afull_bar[s]);
-                    bulk_copy_g2s(st + G::B_OFF, src + abytes, (uint32_t)kBBytes, &afull_bar[s]);
+                    mbar_expect_tx(&full_bar[s], abytes);
+                    bulk_copy_g2s(ring + (size_t)s * G::STAGE, src, abytes, &full_bar[s]);
                 }
             }
         }
@@ -475,7 +509,16 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
             constexpr uint32_t idesc = idesc_f16(kTP, G::N);
-            uint32_t g = 0, gp = 0;
+            // descriptors: the upper 32 bits are the same for every operand; the address
+            // field of the lower ones is linear in the shared address (16-byte units; shared
+            // addresses stay below 2^18, so the 14-bit field never carries)
+            const uint64_t sdb = sdesc(smem_u32(ring));
+            const uint32_t dhi = (uint32_t)(sdb >> 32), dlo0 = (uint32_t)sdb;
+            auto dsc = [&](uint32_t lo, uint32_t off) -> uint64_t {
+                return ((uint64_t)dhi << 32) | (uint64_t)(lo + (off >> 4));
+            };
+            uint32_t s = 0, sph = 0, gp = 0;  // stage slot and its phase parity; pass count
+            uint32_t dlo = dlo0;              // lower descriptor half of slot s
             bool ok = true;
             UnitWalk walk(a, units);
             for (uint32_t u = blockIdx.x; u < units && ok; u += gridDim.x) {
@@ -490,35 +533,35 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                         tc_fence_after();
                         const uint32_t d0 = tmem + buf * kBufCols;
                         const uint32_t kb1 = min(w.nkb, kb0 + (uint32_t)kPassKB);
-                        for (uint32_t kb = kb0; kb < kb1; ++kb, ++g) {
-                            const uint32_t s = g % S, use = g / S;
-                            if (!mbar_wait(&full_bar[s], use & 1u, &s_abort, a.status)) {
+                        for (uint32_t kb = kb0; kb < kb1; ++kb) {
+                            if (!mbar_wait(&full_bar[s], sph, &s_abort, a.status)) {
                                 ok = false;
                                 break;
                             }
                             tc_fence_after();
-                            // descriptors are linear in the address field: the stage's base
-                            // descriptor plus the operand's offset in 16-byte units (shared
-                            // addresses stay below 2^18, so the 14-bit field never carries)
-                            const uint64_t sd0 = sdesc(smem_u32(ring + (size_t)s * G::STAGE));
                             const uint32_t acc0 = kb > kb0 ? 1u : 0u;
                             // [Br; Bi] = Z rows NM.., [-Bi; Br] = Z rows 0..
-                            const uint64_t bd[4] = {
-                                sd0 + ((G::Z_OFF + G::NM * 32) >> 4),
-                                sd0 + ((G::Z_OFF + G::Z_BYTES + G::NM * 32) >> 4),
-                                sd0 + (G::Z_OFF >> 4), sd0 + ((G::Z_OFF + G::Z_BYTES) >> 4)};
+                            const uint64_t bd[4] = {dsc(dlo, G::Z_OFF + G::NM * 32),
+                                                    dsc(dlo, G::Z_OFF + G::Z_BYTES + G::NM * 32),
+                                                    dsc(dlo, G::Z_OFF),
+                                                    dsc(dlo, G::Z_OFF + G::Z_BYTES)};
                             // one complex product: D += A_g (re, im) x Z window, split FP16
-                            auto cplx = [&](uint32_t d, int ga) {
-                                const uint32_t ao = (uint32_t)(4 * ga) * G::A_BYTES;
-                                const uint64_t ad[4] = {
-                                    sd0 + (ao >> 4), sd0 + ((ao + G::A_BYTES) >> 4),
-                                    sd0 + ((ao + 2 * G::A_BYTES) >> 4),
-                                    sd0 + ((ao + 3 * G::A_BYTES) >> 4)};
+                            auto cplx = [&](uint32_t d, uint32_t ao) {
+                                const uint64_t ad[4] = {dsc(dlo, ao), dsc(dlo, ao + G::A_BYTES),
+                                                        dsc(dlo, ao + 2 * G::A_BYTES),
+                                                        dsc(dlo, ao + 3 * G::A_BYTES)};
                                 mma_cplx6(d, ad, bd, idesc, acc0);
                             };
-                            cplx(d0, 0);  // [XC | XS], [C | S], or [C2 | S2]
-                            if (GEN && ph == 0) cplx(d0 + (uint32_t)G::N, 1);  // [YC | YS]
+                            cplx(d0, 0u);  // [XC | XS], [C | S], or [C2 | S2]
+                            if (GEN && ph == 0) cplx(d0 + (uint32_t)G::N, 4u * G::A_BYTES);  // [YC | YS]
                             mma_commit(&empty_bar[s]);
+                            if (++s == (uint32_t)S) {
+                                s = 0;
+                                sph ^= 1u;
+                                dlo = dlo0;
+                            } else {
+                                dlo += (uint32_t)G::STAGE >> 4;
+                            }
                         }
                         if (ok) mma_commit(&pfull_bar[buf]);
                     }
@@ -532,7 +575,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
         }
         __syncwarp();
     } else {
-        // ---------------- fold and epilogue (warps 0-3 and 10-13) ----------------
+        // ---------------- fold and epilogue ----------------
         // warp w may access TMEM lanes 32 (w % 4) ..; the two warps of a lane quarter split
         // the coarse steps: warp half eh owns m in [eh NM/2, (eh+1) NM/2), i.e. the same
         // half of every NM-column quantity block, in the folds and in the power pass, so a
@@ -609,7 +652,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             // quantities: phase 0 groups (re, im) then phase 1 (re, im)
             constexpr int NQ = GEN ? 6 : 4;
             // the standard variant loads chunk m0 + 8 while it computes chunk m0
-            constexpr bool PREFETCH = !GEN;
+            constexpr bool PREFETCH = !GEN && kThreads <= 512;
             uint32_t x[NQ][8];
             auto load_chunk = [&](int m0) {
 #pragma unroll
@@ -685,7 +728,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
 
 // The operand table: one CTA per (K-block, phase) builds the K-block's A matrices for
 // p < 128, split FP16 (group g, re / im, hi / lo) in the layout the tensor kernel stages,
-// followed by the 16 observations' frequency steps b, and copies them out coalesced.
+// and copies them out coalesced; the phase-0 CTA also writes the 16 frequency steps b.
 //   phase 0: v0 tsc0 exp(i alpha) (and v1 tsc1 exp(i alpha), generalized)
 //   phase 1: exp(2i alpha) (standard) or v0 tsc0 exp(2i alpha) (generalized)
 // with alpha = a + p b in 64-bit fixed point. Observations past the object's end get zero
@@ -748,17 +791,17 @@ __global__ void __launch_bounds__(256) agen_kernel(MixedArgs a, uint32_t total_k
             }
         }
     }
-    if (threadIdx.x < (uint32_t)kTK) {
+    if (ph == 0 && threadIdx.x < (uint32_t)kTK) {
         const uint32_t j = threadIdx.x;
         uint2 b = make_uint2(0u, 0u);
         if (j < cnt) b = make_uint2(rec[j].b_lo, rec[j].b_hi);
-        *reinterpret_cast<uint2 *>(ts + abytes + 8u * j) = b;
+        reinterpret_cast<uint2 *>(const_cast<void *>(a.steps))[(uint64_t)kbg * kTK + j] = b;
     }
     __syncthreads();
     uint4 *dst = reinterpret_cast<uint4 *>(static_cast<unsigned char *>(const_cast<void *>(a.optab)) +
                                            (uint64_t)kbg * G::KB_BYTES + (ph ? G::T0_BYTES : 0));
     const uint4 *src = reinterpret_cast<const uint4 *>(ts);
-    for (uint32_t i = threadIdx.x; i < (abytes + (uint32_t)kBBytes) / 16u; i += blockDim.x) dst[i] = src[i];
+    for (uint32_t i = threadIdx.x; i < abytes / 16u; i += blockDim.x) dst[i] = src[i];
 }
 
 template <bool GEN>
@@ -785,7 +828,8 @@ uint32_t tensor_tile_freqs(int variant) {
 size_t tensor_smem_bytes(int variant) { return variant ? tensor_smem<true>() : tensor_smem<false>(); }
 
 size_t tensor_optab_bytes(int variant, uint64_t total_kb) {
-    return (size_t)total_kb * (size_t)(variant ? TGeo<true>::KB_BYTES : TGeo<false>::KB_BYTES);
+    return (size_t)total_kb *
+           ((size_t)(variant ? TGeo<true>::KB_BYTES : TGeo<false>::KB_BYTES) + kTensorStepBytes);
 }
 
 cudaError_t launch_tensor_optab(int variant, const MixedArgs &a, uint64_t total_kb, cudaStream_t st) {
