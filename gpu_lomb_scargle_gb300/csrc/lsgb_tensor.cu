@@ -354,12 +354,12 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
 
     if (tid == 0) {
         for (int s = 0; s < S; ++s) {
-            mbar_init(&full_bar[s], kProducerThreads + 1);
+            mbar_init(&full_bar[s], kProducerWarps + 1);  // one arrival per producer warp
             mbar_init(&empty_bar[s], 1);
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(&pfull_bar[b], 1);
-            mbar_init(&pempty_bar[b], kEpilogueThreads);
+            mbar_init(&pempty_bar[b], kEpilogueThreads / 32);  // one arrival per warp
         }
         mbar_init(&drain_bar, 1);
         s_abort = 0u;
@@ -404,7 +404,10 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             for (uint32_t h = 0; h < JPT / 2; ++h) nb[h] = __ldg(steps + (kbg * kTK + j0) / 2u + h);
         };
         if (blockIdx.x < units) load_b(walk.nxt.kb0);
-        for (uint32_t u = blockIdx.x; u < units && !s_abort; u += gridDim.x) {
+        // the warp's lanes leave together: the abort flag as lane 0 reads it, and every
+        // wait's outcome voted over the warp
+        for (uint32_t u = blockIdx.x; u < units && __shfl_sync(0xffffffffu, s_abort, 0) == 0u;
+             u += gridDim.x) {
             const UnitInfo w = walk.next(a, u, units);
             const uint32_t k = w.tile * (uint32_t)G::TILE + 128u * m;
             for (uint32_t ks = 0; ks < 2u * w.nkb; ++ks, ++g) {
@@ -418,7 +421,9 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                     load_b(w.kb0 + (ks1 < w.nkb ? ks1 : ks1 - w.nkb));
                 else if (u + gridDim.x < units)
                     load_b(walk.nxt.kb0);
-                if (!mbar_wait(&empty_bar[s], (us & 1u) ^ 1u, &s_abort, a.status)) break;
+                if (!__all_sync(0xffffffffu,
+                                mbar_wait(&empty_bar[s], (us & 1u) ^ 1u, &s_abort, a.status)))
+                    break;
                 unsigned char *st = ring + (size_t)s * G::STAGE;
                 // packed FP16 pairs (j, j + 1) of cos and sin, hi and lo
                 uint32_t pch[JPT / 2], pcl[JPT / 2], psh[JPT / 2], psl[JPT / 2];
@@ -467,9 +472,11 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                 put(zh + kRowNM + G::Z_BYTES, pcl);
                 put(zh + 2u * kRowNM, psh);
                 put(zh + 2u * kRowNM + G::Z_BYTES, psl);
-                // generic-proxy stores -> the MMA's async-proxy reads
+                // generic-proxy stores -> the MMA's async-proxy reads; then one arrival for
+                // the warp, after all its lanes have fenced
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                mbar_arrive(&full_bar[s]);
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&full_bar[s]);
             }
         }
     } else if (warp == kLoaderWarp) {
@@ -599,7 +606,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                 const uint32_t wcols = ph ? (uint32_t)G::W1 : (uint32_t)G::W0;
                 for (uint32_t pi = 0; pi < npass; ++pi, ++gp) {
                     const uint32_t buf = gp & 1u, ub = gp >> 1;
-                    if (!mbar_wait(&pfull_bar[buf], ub & 1u, &s_abort, a.status)) {
+                    if (!__all_sync(0xffffffffu, mbar_wait(&pfull_bar[buf], ub & 1u, &s_abort, a.status))) {
                         ok = false;
                         break;
                     }
@@ -633,7 +640,8 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                     }
                     tmem_wait_st();
                     tc_fence_before();
-                    mbar_arrive(&pempty_bar[buf]);
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&pempty_bar[buf]);
                 }
             }
             if (!ok) break;
