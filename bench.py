@@ -55,11 +55,11 @@ TENSOR_FLOPS_PER_PAIR_STD = 48
 CUDA_CORE_SHAPE_STD = (12, 256, 2, 2, 0)
 OPS_PER_PAIR_CUDA_CORE = 76 / 12
 # DRAM read + write bytes of one tensor-kernel launch, from the ncu capture of the same
-# batch at 1e5 frequencies (profiles/tensor_kernel_std_999obj_1e5freq.md): the ObsRec
-# records and per-object tables are read from DRAM once per launch whatever the grid
-# size (re-reads across frequency tiles hit L2), and nothing is written without a
-# periodogram
-TENSOR_DRAM_BYTES_PER_LAUNCH = 5.78e6
+# batch at 1e5 frequencies (profiles/tensor_kernel_std_999obj_1e5freq.md): the operand
+# table (32 KB of split-FP16 left operands per K-block, 11,487 K-blocks: 376 MB) is read
+# from DRAM once per launch whatever the grid size, because the units of one object run
+# back to back and re-read it from L2; nothing is written without a periodogram
+TENSOR_DRAM_BYTES_PER_LAUNCH = 3.84e8
 MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_BF16_TFLOPS = 1900.0
 L2_FLUSH_BYTES = 256 << 20
