@@ -299,7 +299,7 @@ int enqueue_batch(Batch &b, Workspace &ws, cudaStream_t st, cudaEvent_t ev0, cud
         MixedArgs a{};
         a.rec = ws.rec.p;
         a.steps = ws.optab.p;
-        a.optab = (const unsigned char *)ws.optab.p + b.total_kb * kTensorStepBytes;
+        a.optab = (const unsigned char *)ws.optab.p + b.total_kb * tensor_step_bytes(b.variant);
         a.objs = d_objs;
         a.perm = (const uint32_t *)ws.perm.p;
         a.n_obj = b.n_obj;

@@ -96,7 +96,7 @@ struct MixedArgs {
     uint32_t *status;      // tensor form: bit 0 set when a bounded pipeline wait timed out
                            // (may be null)
     const void *optab;     // tensor form: the operand table's A matrices, and
-    const void *steps;     // the K-blocks' frequency steps (kTensorStepBytes each); both
+    const void *steps;     // the K-blocks' steps arrays (tensor_step_bytes each); both
                            // filled by launch_tensor_optab for this batch
 };
 
@@ -153,14 +153,16 @@ uint32_t tensor_tile_freqs(int variant);
 size_t tensor_smem_bytes(int variant);
 cudaError_t launch_tensor(int variant, int dtype, const MixedArgs &a, int grid, cudaStream_t st);
 // The tensor form's operand table: for every K-block (16 observations) of every object and
-// both phases, the tile-independent left operand v exp(i (a + p b)) (phase 0) or
-// (v) exp(2i (a + p b)) (phase 1) for p < 128, split into FP16 hi / lo matrices in the
-// kernel's shared-memory layout; and the K-block's 16 frequency steps b (64-bit, zero past
-// the object's end). One buffer of tensor_optab_bytes: the steps of all K-blocks
-// (total_kb x kTensorStepBytes) at its start, the A matrices after them. Needs the records.
-// total_kb = sum over objects of ceil(n / 16); ObjInfo::kb0 must hold the prefix sums.
+// both phases, the tile-independent left operand exp(i (a + p b)) (phase 0; times v0 for
+// the standard variant) or exp(2i (a + p b)) (phase 1) for p < 128, split into FP16 hi / lo
+// matrices in the kernel's shared-memory layout; and the K-block's steps array: the 16
+// frequency steps b (64-bit), with the generalized variant's two scaled weights (zero past
+// the object's end). One buffer of tensor_optab_bytes: the steps arrays of all K-blocks
+// (total_kb x tensor_step_bytes) at its start, the A matrices after them. Needs the
+// records. total_kb = sum over objects of ceil(n / 16); ObjInfo::kb0 must hold the prefix
+// sums.
 constexpr uint32_t kTensorKBlock = 16;
-constexpr uint32_t kTensorStepBytes = kTensorKBlock * 8;
+size_t tensor_step_bytes(int variant);
 size_t tensor_optab_bytes(int variant, uint64_t total_kb);
 cudaError_t launch_tensor_optab(int variant, const MixedArgs &a, uint64_t total_kb, cudaStream_t st);
 // Compiled mixed shapes as (variant, F, threads, min CTAs, packed, unroll); returns the count.

@@ -79,22 +79,28 @@ constexpr long long kWaitCycles = 1ll << 32;  // ~2 s at 2 GHz
 template <bool GEN>
 struct TGeo {
     static constexpr int NM = GEN ? 32 : 64;       // coarse frequency steps m per unit
-    static constexpr int N = 2 * NM;               // MMA N: [real | imaginary]
-    static constexpr int NAG0 = GEN ? 2 : 1;       // phase-0 A groups: v e^ia (, v1 e^ia)
-    static constexpr int W0 = NAG0 * N;            // phase-0 accumulator columns
-    static constexpr int W1 = N;                   // phase-1 accumulator columns
+    // right-operand groups of phase 0: standard 1 (the weight v0 is on the A side);
+    // generalized 2, B1 = v0 e^{i gamma} and B2 = v1 e^{i gamma} against one unweighted A
+    static constexpr int G0 = GEN ? 2 : 1;
+    static constexpr int N0 = 2 * G0 * NM;         // phase-0 MMA N: [Re groups | Im groups]
+    static constexpr int N1 = 2 * NM;              // phase-1 MMA N: [Re | Im]
+    static constexpr int W0 = N0;                  // phase-0 accumulator columns
+    static constexpr int W1 = N1;                  // phase-1 accumulator columns
     static constexpr int A_BYTES = kTP * kTK * 2;  // one 128 x 16 FP16 matrix
-    static constexpr int Z_ROWS = 3 * NM;
+    static constexpr int Z_ROWS = 3 * G0 * NM;     // [-Bi; Br; Bi], each G rows blocks of NM
     static constexpr int Z_BYTES = Z_ROWS * kTK * 2;
-    // stage: A matrices (group g, re/im, hi/lo), then the Z matrix (hi, lo)
-    static constexpr int Z_OFF = NAG0 * 4 * A_BYTES;
+    // stage: the A matrices (re/im, hi/lo), then the Z matrix (hi, lo)
+    static constexpr int Z_OFF = 4 * A_BYTES;
     static constexpr int STAGE = (Z_OFF + 2 * Z_BYTES + 1023) / 1024 * 1024;
-    static constexpr int STAGES = GEN ? 5 : 7;
+    static constexpr int STAGES = 7;
     static constexpr int TILE = kTP * NM;          // frequencies per unit
-    // operand table, per K-block: the A matrices of phase 0 (NAG0 groups), then of phase 1
-    static constexpr int T0_BYTES = Z_OFF;
+    // operand table, per K-block: the A matrices of phase 0, then of phase 1
+    static constexpr int T0_BYTES = 4 * A_BYTES;
     static constexpr int T1_BYTES = 4 * A_BYTES;
     static constexpr int KB_BYTES = T0_BYTES + T1_BYTES;
+    // bytes per observation of the steps array: b (standard), b and the two scaled
+    // weights (generalized)
+    static constexpr int SB = GEN ? 16 : 8;
     // producers: one row m and JPT consecutive observations per thread; the K-block's 16
     // observations in JS slices
     static constexpr int JPT = NM * kTK / kProducerThreads;
@@ -391,17 +397,20 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
         const uint32_t c = ((uint32_t)lane >> 3) + 4u * (uint32_t)(warp - kProducerWarp0);
         const uint32_t m = 8u * (c / JS) + ((uint32_t)lane & 7u);
         const uint32_t j0 = JPT * (c % JS);
-        // rows m (-Bi), NM + m (Br), 2 NM + m (Bi) of the hi matrix; lo is Z_BYTES further
+        // group g of G: rows g NM + m (-Bi), (G + g) NM + m (Br), (2G + g) NM + m (Bi) of the
+        // hi matrix; lo is Z_BYTES further
         const uint32_t zo = (uint32_t)G::Z_OFF + kmaj_off(m, j0);
         constexpr uint32_t kRowNM = (uint32_t)G::NM * 32u;  // kmaj_off(r + NM) - kmaj_off(r)
         uint32_t g = 0;
         UnitWalk walk(a, units);
-        // the steps b of the next stage's K-block, loaded one stage ahead
+        // the steps (and weights) of the next stage's K-block, loaded one stage ahead
+        constexpr uint32_t NQ4 = JPT * (uint32_t)G::SB / 16u;  // uint4 per thread and stage
         const uint4 *steps = static_cast<const uint4 *>(a.steps);
-        uint4 nb[JPT / 2];
+        uint4 nb[NQ4];
         auto load_b = [&](uint32_t kbg) {
 #pragma unroll
-            for (uint32_t h = 0; h < JPT / 2; ++h) nb[h] = __ldg(steps + (kbg * kTK + j0) / 2u + h);
+            for (uint32_t h = 0; h < NQ4; ++h)
+                nb[h] = __ldg(steps + (kbg * kTK + j0) * (uint32_t)G::SB / 16u + h);
         };
         if (blockIdx.x < units) load_b(walk.nxt.kb0);
         // the warp's lanes leave together: the abort flag as lane 0 reads it, and every
@@ -413,9 +422,9 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             for (uint32_t ks = 0; ks < 2u * w.nkb; ++ks, ++g) {
                 const bool ph1 = ks >= w.nkb;
                 const uint32_t s = g % S, us = g / S;
-                uint4 cb[JPT / 2];
+                uint4 cb[NQ4];
 #pragma unroll
-                for (uint32_t h = 0; h < JPT / 2; ++h) cb[h] = nb[h];
+                for (uint32_t h = 0; h < NQ4; ++h) cb[h] = nb[h];
                 const uint32_t ks1 = ks + 1u;
                 if (ks1 < 2u * w.nkb)
                     load_b(w.kb0 + (ks1 < w.nkb ? ks1 : ks1 - w.nkb));
@@ -424,13 +433,33 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                 if (!__all_sync(0xffffffffu,
                                 mbar_wait(&empty_bar[s], (us & 1u) ^ 1u, &s_abort, a.status)))
                     break;
-                unsigned char *st = ring + (size_t)s * G::STAGE;
-                // packed FP16 pairs (j, j + 1) of cos and sin, hi and lo
-                uint32_t pch[JPT / 2], pcl[JPT / 2], psh[JPT / 2], psl[JPT / 2];
+                unsigned char *zh = ring + (size_t)s * G::STAGE + zo;
+                auto put = [&](unsigned char *dst, const uint32_t (&v)[JPT / 2]) {
+                    if constexpr (JPT == 8)
+                        *reinterpret_cast<uint4 *>(dst) = make_uint4(v[0], v[1], v[2], v[3]);
+                    else if constexpr (JPT == 4)
+                        *reinterpret_cast<uint2 *>(dst) = make_uint2(v[0], v[1]);
+                    else
+                        *reinterpret_cast<uint32_t *>(dst) = v[0];
+                };
+                // the observations in pairs (j, j + 1): cos / sin of k b_j (or of twice it),
+                // times the group weights, split and packed as FP16 pairs
+                const uint32_t ng = (GEN && !ph1) ? 2u : 1u;
+                uint32_t pch[2][JPT / 2], pcl[2][JPT / 2], psh[2][JPT / 2], psl[2][JPT / 2];
 #pragma unroll
                 for (uint32_t h = 0; h < JPT / 2; ++h) {
-                    const uint32_t bl[2] = {cb[h].x, cb[h].z}, bh[2] = {cb[h].y, cb[h].w};
-                    float ch[2], cl[2], sh[2], sl[2];
+                    uint32_t bl[2], bh[2];
+                    float wt[2][2];  // [observation][group]
+                    if constexpr (GEN) {
+                        const uint4 q0 = cb[2 * h], q1 = cb[2 * h + 1];
+                        bl[0] = q0.x; bh[0] = q0.y; bl[1] = q1.x; bh[1] = q1.y;
+                        wt[0][0] = __uint_as_float(q0.z); wt[0][1] = __uint_as_float(q0.w);
+                        wt[1][0] = __uint_as_float(q1.z); wt[1][1] = __uint_as_float(q1.w);
+                    } else {
+                        bl[0] = cb[h].x; bh[0] = cb[h].y; bl[1] = cb[h].z; bh[1] = cb[h].w;
+                        wt[0][0] = wt[0][1] = wt[1][0] = wt[1][1] = 1.0f;
+                    }
+                    float ch[2][2], cl[2][2], sh[2][2], sl[2][2];  // [group][observation]
 #pragma unroll
                     for (int q = 0; q < 2; ++q) {
                         // hi 32 bits of k b mod 2^64: (k b_lo) >> 32 plus k b_hi
@@ -442,36 +471,38 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                             sn = 2.0f * cs * sn;
                             cs = c2;
                         }
-                        vsplit(cs, ch[q], cl[q]);
-                        vsplit(sn, sh[q], sl[q]);
-                    }
-                    pch[h] = pack_h2(ch[0], ch[1]);
-                    pcl[h] = pack_h2(cl[0], cl[1]);
-                    psh[h] = pack_h2(sh[0], sh[1]);
-                    psl[h] = pack_h2(sl[0], sl[1]);
-                }
-                // -x = (-hi) + (-lo) exactly: the sign bits of both FP16 halves flipped
-                uint32_t nsh[JPT / 2], nsl[JPT / 2];
 #pragma unroll
-                for (uint32_t h = 0; h < JPT / 2; ++h) {
-                    nsh[h] = psh[h] ^ 0x80008000u;
-                    nsl[h] = psl[h] ^ 0x80008000u;
+                        for (int gi = 0; gi < (GEN ? 2 : 1); ++gi) {
+                            vsplit(cs * wt[q][gi], ch[gi][q], cl[gi][q]);
+                            vsplit(sn * wt[q][gi], sh[gi][q], sl[gi][q]);
+                        }
+                    }
+#pragma unroll
+                    for (int gi = 0; gi < (GEN ? 2 : 1); ++gi) {
+                        pch[gi][h] = pack_h2(ch[gi][0], ch[gi][1]);
+                        pcl[gi][h] = pack_h2(cl[gi][0], cl[gi][1]);
+                        psh[gi][h] = pack_h2(sh[gi][0], sh[gi][1]);
+                        psl[gi][h] = pack_h2(sl[gi][0], sl[gi][1]);
+                    }
                 }
-                unsigned char *zh = st + zo;
-                auto put = [&](unsigned char *dst, const uint32_t (&v)[JPT / 2]) {
-                    if constexpr (JPT == 8)
-                        *reinterpret_cast<uint4 *>(dst) = make_uint4(v[0], v[1], v[2], v[3]);
-                    else if constexpr (JPT == 4)
-                        *reinterpret_cast<uint2 *>(dst) = make_uint2(v[0], v[1]);
-                    else
-                        *reinterpret_cast<uint32_t *>(dst) = v[0];
-                };
-                put(zh, nsh);
-                put(zh + G::Z_BYTES, nsl);
-                put(zh + kRowNM, pch);
-                put(zh + kRowNM + G::Z_BYTES, pcl);
-                put(zh + 2u * kRowNM, psh);
-                put(zh + 2u * kRowNM + G::Z_BYTES, psl);
+#pragma unroll
+                for (uint32_t gi = 0; gi < (GEN ? 2u : 1u); ++gi) {
+                    if (gi >= ng) break;
+                    // -x = (-hi) + (-lo) exactly: the sign bits of both FP16 halves flipped
+                    uint32_t nsh[JPT / 2], nsl[JPT / 2];
+#pragma unroll
+                    for (uint32_t h = 0; h < JPT / 2; ++h) {
+                        nsh[h] = psh[gi][h] ^ 0x80008000u;
+                        nsl[h] = psl[gi][h] ^ 0x80008000u;
+                    }
+                    unsigned char *zg = zh + gi * kRowNM;
+                    put(zg, nsh);
+                    put(zg + G::Z_BYTES, nsl);
+                    put(zg + ng * kRowNM, pch[gi]);
+                    put(zg + ng * kRowNM + G::Z_BYTES, pcl[gi]);
+                    put(zg + 2u * ng * kRowNM, psh[gi]);
+                    put(zg + 2u * ng * kRowNM + G::Z_BYTES, psl[gi]);
+                }
                 // generic-proxy stores -> the MMA's async-proxy reads; then one arrival for
                 // the warp, after all its lanes have fenced
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -515,7 +546,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
     } else if (warp == 4) {
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
-            constexpr uint32_t idesc = idesc_f16(kTP, G::N);
+            constexpr uint32_t idesc0 = idesc_f16(kTP, G::N0), idesc1 = idesc_f16(kTP, G::N1);
             // descriptors: the upper 32 bits are the same for every operand; the address
             // field of the lower ones is linear in the shared address (16-byte units; shared
             // addresses stay below 2^18, so the 14-bit field never carries)
@@ -547,20 +578,19 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                             }
                             tc_fence_after();
                             const uint32_t acc0 = kb > kb0 ? 1u : 0u;
-                            // [Br; Bi] = Z rows NM.., [-Bi; Br] = Z rows 0..
-                            const uint64_t bd[4] = {dsc(dlo, G::Z_OFF + G::NM * 32),
-                                                    dsc(dlo, G::Z_OFF + G::Z_BYTES + G::NM * 32),
+                            // windows of Z = [-Bi; Br; Bi] (blocks of G NM rows): [Br; Bi] at
+                            // row G NM, [-Bi; Br] at row 0
+                            const uint32_t gnm = ph ? 1u : (uint32_t)G::G0;
+                            const uint32_t wre = (uint32_t)G::Z_OFF + gnm * (uint32_t)G::NM * 32u;
+                            const uint64_t bd[4] = {dsc(dlo, wre), dsc(dlo, wre + G::Z_BYTES),
                                                     dsc(dlo, G::Z_OFF),
                                                     dsc(dlo, G::Z_OFF + G::Z_BYTES)};
-                            // one complex product: D += A_g (re, im) x Z window, split FP16
-                            auto cplx = [&](uint32_t d, uint32_t ao) {
-                                const uint64_t ad[4] = {dsc(dlo, ao), dsc(dlo, ao + G::A_BYTES),
-                                                        dsc(dlo, ao + 2 * G::A_BYTES),
-                                                        dsc(dlo, ao + 3 * G::A_BYTES)};
-                                mma_cplx6(d, ad, bd, idesc, acc0);
-                            };
-                            cplx(d0, 0u);  // [XC | XS], [C | S], or [C2 | S2]
-                            if (GEN && ph == 0) cplx(d0 + (uint32_t)G::N, 4u * G::A_BYTES);  // [YC | YS]
+                            // one complex product: D += A (re, im) x Z window, split FP16:
+                            // [XC | XS], [C C' | S S'] (generalized phase 0), or [C2 | S2]
+                            const uint64_t ad[4] = {dsc(dlo, 0u), dsc(dlo, G::A_BYTES),
+                                                    dsc(dlo, 2 * G::A_BYTES),
+                                                    dsc(dlo, 3 * G::A_BYTES)};
+                            mma_cplx6(d0, ad, bd, ph ? idesc1 : idesc0, acc0);
                             mma_commit(&empty_bar[s]);
                             if (++s == (uint32_t)S) {
                                 s = 0;
@@ -667,7 +697,9 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                 for (int k = 0; k < NQ; ++k) {
                     const bool p1 = k >= NQ - 2;
                     const int kk = p1 ? k - (NQ - 2) : k;
-                    const uint32_t col = (uint32_t)((kk >> 1) * G::N + (kk & 1) * G::NM + m0);
+                    // phase 0: group g = kk / 2 of G0, re / im = kk % 2 in [Re groups | Im groups]
+                    const uint32_t gq = p1 ? 1u : (uint32_t)G::G0;
+                    const uint32_t col = (uint32_t)(kk & 1) * gq * G::NM + (uint32_t)(kk >> 1) * G::NM + (uint32_t)m0;
                     tmem_ld8((p1 ? run2 : run1) + col, x[k]);
                 }
             };
@@ -735,12 +767,13 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
 }
 
 // The operand table: one CTA per (K-block, phase) builds the K-block's A matrices for
-// p < 128, split FP16 (group g, re / im, hi / lo) in the layout the tensor kernel stages,
-// and copies them out coalesced; the phase-0 CTA also writes the 16 frequency steps b.
-//   phase 0: v0 tsc0 exp(i alpha) (and v1 tsc1 exp(i alpha), generalized)
-//   phase 1: exp(2i alpha) (standard) or v0 tsc0 exp(2i alpha) (generalized)
+// p < 128, split FP16 (re / im, hi / lo) in the layout the tensor kernel stages, and copies
+// them out coalesced; the phase-0 CTA also writes the K-block's steps array entries.
+//   standard:    phase 0 v0 tsc0 exp(i alpha), phase 1 exp(2i alpha); steps {b}
+//   generalized: phase 0 exp(i alpha),         phase 1 exp(2i alpha); steps {b, v0 tsc0,
+//                v1 tsc1} (the weights go on the right operand, built by the producers)
 // with alpha = a + p b in 64-bit fixed point. Observations past the object's end get zero
-// A entries (and b = 0), so they add nothing to any product.
+// A entries (and zero steps and weights), so they add nothing to any product.
 template <bool GEN>
 __global__ void __launch_bounds__(256) agen_kernel(MixedArgs a, uint32_t total_kb) {
     using G = TGeo<GEN>;
@@ -758,11 +791,9 @@ __global__ void __launch_bounds__(256) agen_kernel(MixedArgs a, uint32_t total_k
     const uint32_t cnt = min((uint32_t)kTK, ob.n - kb * kTK);
     const ObsRec *rec = static_cast<const ObsRec *>(a.rec) + ob.row0 + (uint64_t)kb * kTK;
     const float sc0 = ob.tsc0, sc1 = ob.tsc1;
-    const uint32_t nag = ph ? 1u : (uint32_t)G::NAG0;
-    const uint32_t abytes = nag * 4u * G::A_BYTES;
     for (uint32_t e = threadIdx.x; e < (uint32_t)kTP * (kTK / 4); e += blockDim.x) {
         const uint32_t p = e >> 2, j0 = 4u * (e & 3u);
-        float x[2][2][4];  // [group][re / im][observation]
+        float x[2][4];  // [re / im][observation]
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const uint32_t j = j0 + (uint32_t)q;
@@ -773,43 +804,43 @@ __global__ void __launch_bounds__(256) agen_kernel(MixedArgs a, uint32_t total_k
             turn_sincos(t32, sn, cs);
             const float mk = j < cnt ? 1.0f : 0.0f;
             if (ph == 0) {
-                const float v0 = r.v0 * sc0 * mk, v1 = r.v1 * sc1 * mk;
-                x[0][0][q] = v0 * cs;
-                x[0][1][q] = v0 * sn;
-                x[1][0][q] = v1 * cs;
-                x[1][1][q] = v1 * sn;
+                const float v = (GEN ? 1.0f : r.v0 * sc0) * mk;
+                x[0][q] = v * cs;
+                x[1][q] = v * sn;
             } else {
-                const float wt = (GEN ? r.v0 * sc0 : 1.0f) * mk;
-                x[0][0][q] = wt * fmaf(cs, cs, -sn * sn);
-                x[0][1][q] = wt * (2.0f * cs * sn);
-                x[1][0][q] = 0.0f;
-                x[1][1][q] = 0.0f;
+                x[0][q] = mk * fmaf(cs, cs, -sn * sn);
+                x[1][q] = mk * (2.0f * cs * sn);
             }
         }
-        for (uint32_t gi = 0; gi < nag; ++gi) {
 #pragma unroll
-            for (int c = 0; c < 2; ++c) {
-                float h4[4], l4[4];
+        for (int c = 0; c < 2; ++c) {
+            float h4[4], l4[4];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) vsplit(x[gi][c][q], h4[q], l4[q]);
-                unsigned char *base = ts + (4u * gi + 2u * (uint32_t)c) * G::A_BYTES + kmaj_off(p, j0);
-                *reinterpret_cast<uint2 *>(base) = make_uint2(pack_h2(h4[0], h4[1]), pack_h2(h4[2], h4[3]));
-                *reinterpret_cast<uint2 *>(base + G::A_BYTES) =
-                    make_uint2(pack_h2(l4[0], l4[1]), pack_h2(l4[2], l4[3]));
-            }
+            for (int q = 0; q < 4; ++q) vsplit(x[c][q], h4[q], l4[q]);
+            unsigned char *base = ts + 2u * (uint32_t)c * G::A_BYTES + kmaj_off(p, j0);
+            *reinterpret_cast<uint2 *>(base) = make_uint2(pack_h2(h4[0], h4[1]), pack_h2(h4[2], h4[3]));
+            *reinterpret_cast<uint2 *>(base + G::A_BYTES) =
+                make_uint2(pack_h2(l4[0], l4[1]), pack_h2(l4[2], l4[3]));
         }
     }
     if (ph == 0 && threadIdx.x < (uint32_t)kTK) {
         const uint32_t j = threadIdx.x;
-        uint2 b = make_uint2(0u, 0u);
-        if (j < cnt) b = make_uint2(rec[j].b_lo, rec[j].b_hi);
-        reinterpret_cast<uint2 *>(const_cast<void *>(a.steps))[(uint64_t)kbg * kTK + j] = b;
+        const bool in = j < cnt;
+        const uint32_t b_lo = in ? rec[j].b_lo : 0u, b_hi = in ? rec[j].b_hi : 0u;
+        unsigned char *dst = static_cast<unsigned char *>(const_cast<void *>(a.steps)) +
+                             ((uint64_t)kbg * kTK + j) * (uint32_t)G::SB;
+        if (GEN)
+            *reinterpret_cast<uint4 *>(dst) =
+                make_uint4(b_lo, b_hi, __float_as_uint(in ? rec[j].v0 * sc0 : 0.0f),
+                           __float_as_uint(in ? rec[j].v1 * sc1 : 0.0f));
+        else
+            *reinterpret_cast<uint2 *>(dst) = make_uint2(b_lo, b_hi);
     }
     __syncthreads();
     uint4 *dst = reinterpret_cast<uint4 *>(static_cast<unsigned char *>(const_cast<void *>(a.optab)) +
                                            (uint64_t)kbg * G::KB_BYTES + (ph ? G::T0_BYTES : 0));
     const uint4 *src = reinterpret_cast<const uint4 *>(ts);
-    for (uint32_t i = threadIdx.x; i < abytes / 16u; i += blockDim.x) dst[i] = src[i];
+    for (uint32_t i = threadIdx.x; i < (uint32_t)G::T0_BYTES / 16u; i += blockDim.x) dst[i] = src[i];
 }
 
 template <bool GEN>
@@ -835,9 +866,13 @@ uint32_t tensor_tile_freqs(int variant) {
 
 size_t tensor_smem_bytes(int variant) { return variant ? tensor_smem<true>() : tensor_smem<false>(); }
 
+size_t tensor_step_bytes(int variant) {
+    return (size_t)kTK * (size_t)(variant ? TGeo<true>::SB : TGeo<false>::SB);
+}
+
 size_t tensor_optab_bytes(int variant, uint64_t total_kb) {
     return (size_t)total_kb *
-           ((size_t)(variant ? TGeo<true>::KB_BYTES : TGeo<false>::KB_BYTES) + kTensorStepBytes);
+           ((size_t)(variant ? TGeo<true>::KB_BYTES : TGeo<false>::KB_BYTES) + tensor_step_bytes(variant));
 }
 
 cudaError_t launch_tensor_optab(int variant, const MixedArgs &a, uint64_t total_kb, cudaStream_t st) {
