@@ -299,6 +299,7 @@ int enqueue_batch(Batch &b, Workspace &ws, cudaStream_t st, cudaEvent_t ev0, cud
         MixedArgs a{};
         a.rec = ws.rec.p;
         a.steps = ws.optab.p;
+        a.total_kb = (uint32_t)b.total_kb;
         a.optab = (const unsigned char *)ws.optab.p + b.total_kb * tensor_step_bytes(b.variant);
         a.objs = d_objs;
         a.perm = (const uint32_t *)ws.perm.p;

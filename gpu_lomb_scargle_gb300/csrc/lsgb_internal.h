@@ -98,6 +98,7 @@ struct MixedArgs {
     const void *optab;     // tensor form: the operand table's A matrices, and
     const void *steps;     // the K-blocks' steps arrays (tensor_step_bytes each); both
                            // filled by launch_tensor_optab for this batch
+    uint32_t total_kb;     // tensor form: K-blocks of the batch (the table's phase stride)
 };
 
 

@@ -89,15 +89,19 @@ struct TGeo {
     static constexpr int A_BYTES = kTP * kTK * 2;  // one 128 x 16 FP16 matrix
     static constexpr int Z_ROWS = 3 * G0 * NM;     // [-Bi; Br; Bi], each G rows blocks of NM
     static constexpr int Z_BYTES = Z_ROWS * kTK * 2;
-    // stage: the A matrices (re/im, hi/lo), then the Z matrix (hi, lo)
-    static constexpr int Z_OFF = 4 * A_BYTES;
-    static constexpr int STAGE = (Z_OFF + 2 * Z_BYTES + 1023) / 1024 * 1024;
-    static constexpr int STAGES = 7;
+    // stage: KPS consecutive K-blocks of one phase, so that the MMA thread waits and
+    // commits once per 6 KPS MMAs: their A matrices (re/im, hi/lo; AKB bytes each), then
+    // their Z matrices (hi, lo; ZKB bytes each)
+    static constexpr int KPS = 2;
+    static constexpr int AKB = 4 * A_BYTES;
+    static constexpr int ZKB = 2 * Z_BYTES;
+    static constexpr int Z_OFF = KPS * AKB;
+    static constexpr int STAGE = (Z_OFF + KPS * ZKB + 1023) / 1024 * 1024;
+    static constexpr int STAGES = 4;
     static constexpr int TILE = kTP * NM;          // frequencies per unit
-    // operand table, per K-block: the A matrices of phase 0, then of phase 1
-    static constexpr int T0_BYTES = 4 * A_BYTES;
-    static constexpr int T1_BYTES = 4 * A_BYTES;
-    static constexpr int KB_BYTES = T0_BYTES + T1_BYTES;
+    static_assert(kPassKB % KPS == 0, "passes cover whole stages");
+    // operand table: phase-major, [phase][K-block of the batch], AKB bytes each, so a
+    // stage's K-blocks are one contiguous bulk copy
     // bytes per observation of the steps array: b (standard), b and the two scaled
     // weights (generalized)
     static constexpr int SB = GEN ? 16 : 8;
@@ -419,9 +423,12 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
              u += gridDim.x) {
             const UnitInfo w = walk.next(a, u, units);
             const uint32_t k = w.tile * (uint32_t)G::TILE + 128u * m;
-            for (uint32_t ks = 0; ks < 2u * w.nkb; ++ks, ++g) {
+            uint32_t s = 0;
+            for (uint32_t ks = 0; ks < 2u * w.nkb; ++ks) {
                 const bool ph1 = ks >= w.nkb;
-                const uint32_t s = g % S, us = g / S;
+                const uint32_t kb = ph1 ? ks - w.nkb : ks;
+                const uint32_t kbi = kb % (uint32_t)G::KPS;  // K-block within the stage
+                const bool last = kbi == (uint32_t)G::KPS - 1u || kb + 1u == w.nkb;
                 uint4 cb[NQ4];
 #pragma unroll
                 for (uint32_t h = 0; h < NQ4; ++h) cb[h] = nb[h];
@@ -430,10 +437,14 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                     load_b(w.kb0 + (ks1 < w.nkb ? ks1 : ks1 - w.nkb));
                 else if (u + gridDim.x < units)
                     load_b(walk.nxt.kb0);
-                if (!__all_sync(0xffffffffu,
-                                mbar_wait(&empty_bar[s], (us & 1u) ^ 1u, &s_abort, a.status)))
-                    break;
-                unsigned char *zh = ring + (size_t)s * G::STAGE + zo;
+                if (kbi == 0u) {  // a new stage
+                    s = g % S;
+                    const uint32_t us = g / S;
+                    if (!__all_sync(0xffffffffu,
+                                    mbar_wait(&empty_bar[s], (us & 1u) ^ 1u, &s_abort, a.status)))
+                        break;
+                }
+                unsigned char *zh = ring + (size_t)s * G::STAGE + zo + kbi * (uint32_t)G::ZKB;
                 auto put = [&](unsigned char *dst, const uint32_t (&v)[JPT / 2]) {
                     if constexpr (JPT == 8)
                         *reinterpret_cast<uint4 *>(dst) = make_uint4(v[0], v[1], v[2], v[3]);
@@ -503,11 +514,15 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                     put(zg + 2u * ng * kRowNM, psh[gi]);
                     put(zg + 2u * ng * kRowNM + G::Z_BYTES, psl[gi]);
                 }
-                // generic-proxy stores -> the MMA's async-proxy reads; then one arrival for
-                // the warp, after all its lanes have fenced
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&full_bar[s]);
+                // after the stage's last K-block: generic-proxy stores -> the MMA's
+                // async-proxy reads; then one arrival for the warp, after all its lanes
+                // have fenced
+                if (last) {
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&full_bar[s]);
+                    ++g;
+                }
             }
         }
     } else if (warp == kLoaderWarp) {
@@ -516,30 +531,36 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             const unsigned char *tab = static_cast<const unsigned char *>(a.optab);
             uint32_t g = 0;
             UnitWalk walk(a, units);
-            if (blockIdx.x < units)
-                bulk_prefetch_l2(tab + (uint64_t)walk.nxt.kb0 * G::KB_BYTES,
-                                 min(walk.nxt.nkb, kPrefetchKB) * (uint32_t)G::KB_BYTES);
+            const uint64_t tph = (uint64_t)a.total_kb * G::AKB;  // phase stride of the table
+            auto prefetch = [&](uint32_t kbg, uint32_t n) {  // K-blocks kbg.. of both phases
+                bulk_prefetch_l2(tab + (uint64_t)kbg * G::AKB, n * (uint32_t)G::AKB);
+                bulk_prefetch_l2(tab + tph + (uint64_t)kbg * G::AKB, n * (uint32_t)G::AKB);
+            };
+            if (blockIdx.x < units) prefetch(walk.nxt.kb0, min(walk.nxt.nkb, kPrefetchKB));
             for (uint32_t u = blockIdx.x; u < units && !s_abort; u += gridDim.x) {
                 const UnitInfo w = walk.next(a, u, units);
                 // L2: the next unit's first K-blocks now, this unit's further ones as the
                 // phase-0 pass reaches them
-                if (u + gridDim.x < units)
-                    bulk_prefetch_l2(tab + (uint64_t)walk.nxt.kb0 * G::KB_BYTES,
-                                     min(walk.nxt.nkb, kPrefetchKB) * (uint32_t)G::KB_BYTES);
-                for (uint32_t ks = 0; ks < 2u * w.nkb; ++ks, ++g) {
-                    const uint32_t ph = ks >= w.nkb ? 1u : 0u;
-                    const uint32_t kb = ph ? ks - w.nkb : ks;
-                    const uint32_t s = g % S, us = g / S;
-                    if (!ph && kb + kPrefetchKB < w.nkb)
-                        bulk_prefetch_l2(tab + (uint64_t)(w.kb0 + kb + kPrefetchKB) * G::KB_BYTES,
-                                         (uint32_t)G::KB_BYTES);
-                    if (!mbar_wait(&empty_bar[s], (us & 1u) ^ 1u, &s_abort, a.status)) break;
-                    const uint32_t abytes = ph ? (uint32_t)G::T1_BYTES : (uint32_t)G::T0_BYTES;
-                    const unsigned char *src = tab + (uint64_t)(w.kb0 + kb) * G::KB_BYTES +
-                                               (ph ? (uint32_t)G::T0_BYTES : 0u);
-                    mbar_expect_tx(&full_bar[s], abytes);
-                    bulk_copy_g2s(ring + (size_t)s * G::STAGE, src, abytes, &full_bar[s]);
+                if (u + gridDim.x < units) prefetch(walk.nxt.kb0, min(walk.nxt.nkb, kPrefetchKB));
+                bool ok = true;
+                for (uint32_t ph = 0; ph < 2u && ok; ++ph) {
+                    for (uint32_t kb = 0; kb < w.nkb; kb += G::KPS, ++g) {
+                        const uint32_t s = g % S, us = g / S;
+                        const uint32_t cnt = min((uint32_t)G::KPS, w.nkb - kb);
+                        if (!ph && kb + kPrefetchKB < w.nkb)
+                            prefetch(w.kb0 + kb + kPrefetchKB, min(cnt, w.nkb - kb - kPrefetchKB));
+                        if (!mbar_wait(&empty_bar[s], (us & 1u) ^ 1u, &s_abort, a.status)) {
+                            ok = false;
+                            break;
+                        }
+                        const uint32_t bytes = cnt * (uint32_t)G::AKB;
+                        mbar_expect_tx(&full_bar[s], bytes);
+                        bulk_copy_g2s(ring + (size_t)s * G::STAGE,
+                                      tab + ph * tph + (uint64_t)(w.kb0 + kb) * G::AKB, bytes,
+                                      &full_bar[s]);
+                    }
                 }
+                if (!ok) break;
             }
         }
         __syncwarp();
@@ -571,26 +592,33 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                         tc_fence_after();
                         const uint32_t d0 = tmem + buf * kBufCols;
                         const uint32_t kb1 = min(w.nkb, kb0 + (uint32_t)kPassKB);
-                        for (uint32_t kb = kb0; kb < kb1; ++kb) {
+                        // windows of Z = [-Bi; Br; Bi] (blocks of G NM rows): [Br; Bi] at
+                        // row G NM, [-Bi; Br] at row 0
+                        const uint32_t gnm = ph ? 1u : (uint32_t)G::G0;
+                        const uint32_t wre = gnm * (uint32_t)G::NM * 32u;
+                        const uint32_t idesc = ph ? idesc1 : idesc0;
+                        for (uint32_t kb = kb0; kb < kb1; kb += G::KPS) {  // one stage
                             if (!mbar_wait(&full_bar[s], sph, &s_abort, a.status)) {
                                 ok = false;
                                 break;
                             }
                             tc_fence_after();
-                            const uint32_t acc0 = kb > kb0 ? 1u : 0u;
-                            // windows of Z = [-Bi; Br; Bi] (blocks of G NM rows): [Br; Bi] at
-                            // row G NM, [-Bi; Br] at row 0
-                            const uint32_t gnm = ph ? 1u : (uint32_t)G::G0;
-                            const uint32_t wre = (uint32_t)G::Z_OFF + gnm * (uint32_t)G::NM * 32u;
-                            const uint64_t bd[4] = {dsc(dlo, wre), dsc(dlo, wre + G::Z_BYTES),
-                                                    dsc(dlo, G::Z_OFF),
-                                                    dsc(dlo, G::Z_OFF + G::Z_BYTES)};
-                            // one complex product: D += A (re, im) x Z window, split FP16:
-                            // [XC | XS], [C C' | S S'] (generalized phase 0), or [C2 | S2]
-                            const uint64_t ad[4] = {dsc(dlo, 0u), dsc(dlo, G::A_BYTES),
-                                                    dsc(dlo, 2 * G::A_BYTES),
-                                                    dsc(dlo, 3 * G::A_BYTES)};
-                            mma_cplx6(d0, ad, bd, ph ? idesc1 : idesc0, acc0);
+                            const uint32_t cnt = min((uint32_t)G::KPS, kb1 - kb);
+                            for (uint32_t kbi = 0; kbi < cnt; ++kbi) {
+                                const uint32_t acc0 = kb + kbi > kb0 ? 1u : 0u;
+                                const uint32_t ao = kbi * (uint32_t)G::AKB;
+                                const uint32_t zo = (uint32_t)G::Z_OFF + kbi * (uint32_t)G::ZKB;
+                                const uint64_t bd[4] = {dsc(dlo, zo + wre),
+                                                        dsc(dlo, zo + wre + G::Z_BYTES),
+                                                        dsc(dlo, zo), dsc(dlo, zo + G::Z_BYTES)};
+                                // one complex product: D += A (re, im) x Z window, split
+                                // FP16: [XC | XS], [C C' | S S'] (generalized phase 0), or
+                                // [C2 | S2]
+                                const uint64_t ad[4] = {dsc(dlo, ao), dsc(dlo, ao + G::A_BYTES),
+                                                        dsc(dlo, ao + 2 * G::A_BYTES),
+                                                        dsc(dlo, ao + 3 * G::A_BYTES)};
+                                mma_cplx6(d0, ad, bd, idesc, acc0);
+                            }
                             mma_commit(&empty_bar[s]);
                             if (++s == (uint32_t)S) {
                                 s = 0;
@@ -777,7 +805,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
 template <bool GEN>
 __global__ void __launch_bounds__(256) agen_kernel(MixedArgs a, uint32_t total_kb) {
     using G = TGeo<GEN>;
-    __shared__ __align__(16) unsigned char ts[G::T0_BYTES];
+    __shared__ __align__(16) unsigned char ts[G::AKB];
     const uint32_t kbg = blockIdx.x >> 1, ph = blockIdx.x & 1u;
     if (kbg >= total_kb) return;
     // the object of this K-block: the last o with kb0 <= kbg
@@ -838,9 +866,9 @@ __global__ void __launch_bounds__(256) agen_kernel(MixedArgs a, uint32_t total_k
     }
     __syncthreads();
     uint4 *dst = reinterpret_cast<uint4 *>(static_cast<unsigned char *>(const_cast<void *>(a.optab)) +
-                                           (uint64_t)kbg * G::KB_BYTES + (ph ? G::T0_BYTES : 0));
+                                           ((uint64_t)ph * total_kb + kbg) * G::AKB);
     const uint4 *src = reinterpret_cast<const uint4 *>(ts);
-    for (uint32_t i = threadIdx.x; i < (uint32_t)G::T0_BYTES / 16u; i += blockDim.x) dst[i] = src[i];
+    for (uint32_t i = threadIdx.x; i < (uint32_t)G::AKB / 16u; i += blockDim.x) dst[i] = src[i];
 }
 
 template <bool GEN>
@@ -872,7 +900,7 @@ size_t tensor_step_bytes(int variant) {
 
 size_t tensor_optab_bytes(int variant, uint64_t total_kb) {
     return (size_t)total_kb *
-           ((size_t)(variant ? TGeo<true>::KB_BYTES : TGeo<false>::KB_BYTES) + tensor_step_bytes(variant));
+           (2u * (size_t)(variant ? TGeo<true>::AKB : TGeo<false>::AKB) + tensor_step_bytes(variant));
 }
 
 cudaError_t launch_tensor_optab(int variant, const MixedArgs &a, uint64_t total_kb, cudaStream_t st) {
