@@ -742,24 +742,17 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                 for (int k = 0; k < NQ; ++k)
 #pragma unroll
                     for (int i = 0; i < 8; ++i) q[k][i] = __uint_as_float(x[k][i]);
+                // the eight powers first, branch-free, so that their chains interleave
+                float P[8];
                 auto power_at = [&](int i) {
-                    const uint32_t k = kT + pl + (uint32_t)kTP * (uint32_t)(m0 + i);
-                    float P;
                     if (GEN) {
                         const float cb = q[0][i] * s0, sb = q[1][i] * s0;
-                        P = gen_power_sums(cb, sb, fmaf(-ybar, cb, q[2][i] * s1),
-                                           fmaf(-ybar, sb, q[3][i] * s1), q[4][i] * s0,
-                                           q[5][i] * s0) *
-                            nrm;
+                        P[i] = gen_power_sums(cb, sb, fmaf(-ybar, cb, q[2][i] * s1),
+                                              fmaf(-ybar, sb, q[3][i] * s1), q[4][i] * s0,
+                                              q[5][i] * s0) *
+                               nrm;
                     } else {
-                        P = (std_power2_sums(Nf, N2, q[0][i], q[1][i], q[2][i], q[3][i]) * fa) * fb;
-                    }
-                    // a thread visits its frequencies in increasing k, so a strictly larger
-                    // power is the only way to displace its current best (ties keep the
-                    // lower index, as the reference's argmax does)
-                    if (k < a.n_freq) {
-                        if (a.pgram) store_out<OutT>(a.pgram, out0 + k, P);
-                        if (P > bp) { bp = P; bk = k; }
+                        P[i] = (std_power2_sums(Nf, N2, q[0][i], q[1][i], q[2][i], q[3][i]) * fa) * fb;
                     }
                 };
 #pragma unroll
@@ -768,6 +761,28 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                 if (PREFETCH && m0 + 8 < mend) load_chunk(m0 + 8);
 #pragma unroll
                 for (int i = 4; i < 8; ++i) power_at(i);
+                // a thread visits its frequencies in increasing k, so a strictly larger power
+                // is the only way to displace its current best (ties keep the lower index, as
+                // the reference's argmax does)
+                const uint32_t k0 = kT + pl + (uint32_t)kTP * (uint32_t)m0;
+                if (k0 + (uint32_t)kTP * 7u < a.n_freq) {  // the whole chunk is on the grid
+                    if (a.pgram) {
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) store_out<OutT>(a.pgram, out0 + k0 + (uint32_t)kTP * (uint32_t)i, P[i]);
+                    }
+#pragma unroll
+                    for (int i = 0; i < 8; ++i)
+                        if (P[i] > bp) { bp = P[i]; bk = k0 + (uint32_t)kTP * (uint32_t)i; }
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        const uint32_t k = k0 + (uint32_t)kTP * (uint32_t)i;
+                        if (k < a.n_freq) {
+                            if (a.pgram) store_out<OutT>(a.pgram, out0 + k, P[i]);
+                            if (P[i] > bp) { bp = P[i]; bk = k; }
+                        }
+                    }
+                }
             }
             if (a.best_key) {
 #pragma unroll
