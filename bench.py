@@ -407,7 +407,8 @@ def main():
         y32 = np.ascontiguousarray(w.y, np.float32)
         ids = np.ascontiguousarray(w.obj_id, np.uint32)
         ones = np.ones(w.n_rows, np.float32)
-        pg = np.zeros(w.n_obj * w.n_freq, np.float32)
+        pg = np.empty(w.n_obj * w.n_freq, np.float32)
+        pg.fill(0.0)  # touch every page now: first-touch faults are not the library's time
         dt = []
         devnull = os.open(os.devnull, os.O_WRONLY)
         saved = os.dup(1)
