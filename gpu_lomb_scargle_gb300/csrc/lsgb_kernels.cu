@@ -283,31 +283,6 @@ __device__ __forceinline__ void store_out_d(void *pgram, uint64_t i, double p) {
     reinterpret_cast<OutT *>(pgram)[i] = (OutT)p;
 }
 
-// Packed FP32 pairs (Blackwell f32x2): one instruction issues two FP32 lanes' work.
-__device__ __forceinline__ uint64_t ffma2(uint64_t a, uint64_t b, uint64_t c) {
-    uint64_t d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
-__device__ __forceinline__ uint64_t fmul2(uint64_t a, uint64_t b) {
-    uint64_t d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ uint64_t fadd2(uint64_t a, uint64_t b) {
-    uint64_t d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ uint64_t pack2(float lo, float hi) {
-    uint64_t r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-    return r;
-}
-__device__ __forceinline__ void unpack2(uint64_t v, float &lo, float &hi) {
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-
 // Shared-memory record of the packed (X2) loop, expanded from ObsRec at staging:
 //   q0 = {a_lo, a_hi, b_lo, b_hi}
 //   q1 = {v0, v0, cd, sd}            ({y,y} or {w,w}; the single step for the odd chain)

@@ -147,6 +147,21 @@ __device__ __forceinline__ void vsplit(float x, float &hi, float &lo) {
     lo = __fsub_rn(x, hi);
 }
 
+// Split of two FP32 values x (|x| <= 1, packed f32x2) into FP16 pairs hi = x rounded to
+// FP16 and lo = x - hi rounded to FP16 (the subtraction exact in FP32): the accuracy of
+// vsplit, with one conversion instruction per pair.
+__device__ __forceinline__ void split2(uint64_t x, uint32_t &hi, uint32_t &lo) {
+    float a, b;
+    unpack2(x, a, b);
+    const __half2 h = __floats2half2_rn(a, b);
+    const float2 hf = __half22float2(h);
+    float ra, rb;
+    unpack2(fsub2(x, pack2(hf.x, hf.y)), ra, rb);
+    hi = *reinterpret_cast<const uint32_t *>(&h);
+    const __half2 l = __floats2half2_rn(ra, rb);
+    lo = *reinterpret_cast<const uint32_t *>(&l);
+}
+
 // Two FP32 values as one packed FP16 pair (first value in the low half).
 __device__ __forceinline__ uint32_t pack_h2(float a, float b) {
     const __half2 h = __floats2half2_rn(a, b);
@@ -470,30 +485,31 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                         bl[0] = cb[h].x; bh[0] = cb[h].y; bl[1] = cb[h].z; bh[1] = cb[h].w;
                         wt[0][0] = wt[0][1] = wt[1][0] = wt[1][1] = 1.0f;
                     }
-                    float ch[2][2], cl[2][2], sh[2][2], sl[2][2];  // [group][observation]
+                    float sn[2], cs[2];
 #pragma unroll
                     for (int q = 0; q < 2; ++q) {
                         // hi 32 bits of k b mod 2^64: (k b_lo) >> 32 plus k b_hi
                         const uint32_t t32 = __umulhi(k, bl[q]) + k * bh[q];
-                        float sn, cs;
-                        turn_sincos(t32, sn, cs);
-                        if (ph1) {
-                            const float c2 = fmaf(cs, cs, -sn * sn);
-                            sn = 2.0f * cs * sn;
-                            cs = c2;
-                        }
-#pragma unroll
-                        for (int gi = 0; gi < (GEN ? 2 : 1); ++gi) {
-                            vsplit(cs * wt[q][gi], ch[gi][q], cl[gi][q]);
-                            vsplit(sn * wt[q][gi], sh[gi][q], sl[gi][q]);
-                        }
+                        turn_sincos(t32, sn[q], cs[q]);
+                    }
+                    // the two observations as packed pairs; the doubled angle of phase 1
+                    uint64_t C = pack2(cs[0], cs[1]), Sn = pack2(sn[0], sn[1]);
+                    if (ph1) {
+                        const uint64_t C2 = fsub2(fmul2(C, C), fmul2(Sn, Sn));
+                        Sn = fmul2(fadd2(C, C), Sn);
+                        C = C2;
                     }
 #pragma unroll
                     for (int gi = 0; gi < (GEN ? 2 : 1); ++gi) {
-                        pch[gi][h] = pack_h2(ch[gi][0], ch[gi][1]);
-                        pcl[gi][h] = pack_h2(cl[gi][0], cl[gi][1]);
-                        psh[gi][h] = pack_h2(sh[gi][0], sh[gi][1]);
-                        psl[gi][h] = pack_h2(sl[gi][0], sl[gi][1]);
+                        if (gi >= (int)ng) break;  // phase 1 has one group
+                        uint64_t Cg = C, Sg = Sn;
+                        if (GEN) {
+                            const uint64_t W = pack2(wt[0][gi], wt[1][gi]);
+                            Cg = fmul2(C, W);
+                            Sg = fmul2(Sn, W);
+                        }
+                        split2(Cg, pch[gi][h], pcl[gi][h]);
+                        split2(Sg, psh[gi][h], psl[gi][h]);
                     }
                 }
 #pragma unroll
