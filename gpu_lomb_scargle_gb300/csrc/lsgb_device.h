@@ -93,6 +93,30 @@ __device__ __forceinline__ float std_power2_sums(float N, float N2, float xc, fl
     return fmaf(Q + U, d4 * t, (Q - U) * (d1 * (d1 * t)));
 }
 
+// std_power2_sums for two frequencies at once, every argument a packed f32x2 pair (NN and
+// NN2 hold N and N^2 twice): the arithmetic in packed instructions, the reciprocal square
+// root and the reciprocal per lane.
+__device__ __forceinline__ uint64_t std_power2_sums2(uint64_t NN, uint64_t NN2, uint64_t xc,
+                                                     uint64_t xs, uint64_t c2, uint64_t s2) {
+    const uint64_t h = ffma2(c2, c2, fmul2(s2, s2));
+    float h0, h1;
+    unpack2(h, h0, h1);
+    // 1/r where h > 0; where h = 0, U = V (weight z = 1 on V)
+    const uint64_t ir = pack2(h0 > 0.0f ? rsqrtf(h0) : 0.0f, h1 > 0.0f ? rsqrtf(h1) : 0.0f);
+    const uint64_t z = pack2(h0 > 0.0f ? 0.0f : 1.0f, h1 > 0.0f ? 0.0f : 1.0f);
+    const uint64_t r = fmul2(h, ir);
+    const uint64_t xc2 = fmul2(xc, xc), xs2 = fmul2(xs, xs);
+    const uint64_t Q = fadd2(xc2, xs2), V = fsub2(xc2, xs2);
+    const uint64_t u0 = ffma2(c2, V, fmul2(fmul2(s2, xc), fadd2(xs, xs)));
+    const uint64_t U = ffma2(V, z, fmul2(u0, ir));
+    const uint64_t d1 = fadd2(NN, r);
+    const uint64_t d4 = fsub2(NN2, h);
+    float e0, e1;
+    unpack2(fmul2(d1, d4), e0, e1);
+    const uint64_t t = pack2(__fdividef(1.0f, e0), __fdividef(1.0f, e1));
+    return ffma2(fadd2(Q, U), fmul2(d4, t), fmul2(fsub2(Q, U), fmul2(d1, fmul2(d1, t))));
+}
+
 // Generalized power from weight-normalized sums: cb, sb = C/W, S/W; yc, ys the centered
 // YC/W - ybar cb, YS/W - ybar sb; c2, s2 = C2/W, S2/W (sums of w e^{2 i theta}). The
 // covariances of gen_power_f reduce to D = vcc - vss = c2 - cb^2 + sb^2,

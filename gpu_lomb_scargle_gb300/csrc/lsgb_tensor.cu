@@ -727,6 +727,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             const float fa = us0, fb = 0.5f * nrm * us0;
             const float s0 = us0 * invw, s1 = us1 * invw;
             const float Nf = (float)w.n, N2 = Nf * Nf;
+            const uint64_t NN = pack2(Nf, Nf), NN2 = pack2(N2, N2), FA = pack2(fa, fa), FB = pack2(fb, fb);
             const uint64_t out0 = (uint64_t)w.o * a.n_freq;
             float bp = 0.0f;
             uint32_t bk = 0xffffffffu;
@@ -758,7 +759,8 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                 for (int k = 0; k < NQ; ++k)
 #pragma unroll
                     for (int i = 0; i < 8; ++i) q[k][i] = __uint_as_float(x[k][i]);
-                // the eight powers first, branch-free, so that their chains interleave
+                // the eight powers first, branch-free, so that their chains interleave (the
+                // standard variant in packed pairs of frequencies)
                 float P[8];
                 auto power_at = [&](int i) {
                     if (GEN) {
@@ -767,8 +769,15 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                                               fmaf(-ybar, sb, q[3][i] * s1), q[4][i] * s0,
                                               q[5][i] * s0) *
                                nrm;
-                    } else {
-                        P[i] = (std_power2_sums(Nf, N2, q[0][i], q[1][i], q[2][i], q[3][i]) * fa) * fb;
+                    } else if ((i & 1) == 0) {
+                        const uint64_t p2 = fmul2(
+                            fmul2(std_power2_sums2(NN, NN2, pack2(q[0][i], q[0][i + 1]),
+                                                   pack2(q[1][i], q[1][i + 1]),
+                                                   pack2(q[2][i], q[2][i + 1]),
+                                                   pack2(q[3][i], q[3][i + 1])),
+                                  FA),
+                            FB);
+                        unpack2(p2, P[i], P[i + 1]);
                     }
                 };
 #pragma unroll
