@@ -143,6 +143,33 @@ __device__ __forceinline__ float gen_power_sums(float cb, float sb, float yc, fl
     return fmaf(Q + U, d4 * t, (Q - U) * (d1 * (d1 * t)));
 }
 
+// gen_power_sums for two frequencies at once (packed f32x2 pairs).
+__device__ __forceinline__ uint64_t gen_power_sums2(uint64_t cb, uint64_t sb, uint64_t yc,
+                                                    uint64_t ys, uint64_t c2, uint64_t s2) {
+    const uint64_t one = pack2(1.0f, 1.0f), m2 = pack2(-2.0f, -2.0f);
+    const uint64_t cb2 = fmul2(cb, cb), sb2 = fmul2(sb, sb);
+    const uint64_t D = fadd2(fsub2(c2, cb2), sb2);
+    const uint64_t E = ffma2(m2, fmul2(cb, sb), s2);
+    const uint64_t T = fsub2(fsub2(one, cb2), sb2);
+    const uint64_t h = ffma2(D, D, fmul2(E, E));
+    float h0, h1;
+    unpack2(h, h0, h1);
+    // 1/r where h > 0; where h = 0, U = V (weight z = 1 on V)
+    const uint64_t ir = pack2(h0 > 0.0f ? rsqrtf(h0) : 0.0f, h1 > 0.0f ? rsqrtf(h1) : 0.0f);
+    const uint64_t z = pack2(h0 > 0.0f ? 0.0f : 1.0f, h1 > 0.0f ? 0.0f : 1.0f);
+    const uint64_t r = fmul2(h, ir);
+    const uint64_t yc2 = fmul2(yc, yc), ys2 = fmul2(ys, ys);
+    const uint64_t Q = fadd2(yc2, ys2), V = fsub2(yc2, ys2);
+    const uint64_t u0 = ffma2(D, V, fmul2(fmul2(E, yc), fadd2(ys, ys)));
+    const uint64_t U = ffma2(V, z, fmul2(u0, ir));
+    const uint64_t d1 = fadd2(T, r);
+    const uint64_t d4 = fsub2(fmul2(T, T), h);
+    float e0, e1;
+    unpack2(fmul2(d1, d4), e0, e1);
+    const uint64_t t = pack2(__fdividef(1.0f, e0), __fdividef(1.0f, e1));
+    return ffma2(fadd2(Q, U), fmul2(d4, t), fmul2(fsub2(Q, U), fmul2(d1, fmul2(d1, t))));
+}
+
 // Generalized (floating-mean) power from weighted sums with total weight W:
 // the same closed form applied to the weighted covariances, which is
 // source/main.cu:1728-1776 with the second pass expressed by rotating the

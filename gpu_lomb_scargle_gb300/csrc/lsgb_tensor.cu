@@ -728,6 +728,8 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             const float s0 = us0 * invw, s1 = us1 * invw;
             const float Nf = (float)w.n, N2 = Nf * Nf;
             const uint64_t NN = pack2(Nf, Nf), NN2 = pack2(N2, N2), FA = pack2(fa, fa), FB = pack2(fb, fb);
+            const uint64_t S0 = pack2(s0, s0), S1 = pack2(s1, s1), NYB = pack2(-ybar, -ybar);
+            const uint64_t NRM = pack2(nrm, nrm);
             const uint64_t out0 = (uint64_t)w.o * a.n_freq;
             float bp = 0.0f;
             uint32_t bk = 0xffffffffu;
@@ -763,19 +765,19 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                 // standard variant in packed pairs of frequencies)
                 float P[8];
                 auto power_at = [&](int i) {
+                    if ((i & 1) != 0) return;
+                    auto pq = [&](int k) { return pack2(q[k][i], q[k][i + 1]); };
                     if (GEN) {
-                        const float cb = q[0][i] * s0, sb = q[1][i] * s0;
-                        P[i] = gen_power_sums(cb, sb, fmaf(-ybar, cb, q[2][i] * s1),
-                                              fmaf(-ybar, sb, q[3][i] * s1), q[4][i] * s0,
-                                              q[5][i] * s0) *
-                               nrm;
-                    } else if ((i & 1) == 0) {
+                        const uint64_t cb = fmul2(pq(0), S0), sb = fmul2(pq(1), S0);
                         const uint64_t p2 = fmul2(
-                            fmul2(std_power2_sums2(NN, NN2, pack2(q[0][i], q[0][i + 1]),
-                                                   pack2(q[1][i], q[1][i + 1]),
-                                                   pack2(q[2][i], q[2][i + 1]),
-                                                   pack2(q[3][i], q[3][i + 1])),
-                                  FA),
+                            gen_power_sums2(cb, sb, ffma2(NYB, cb, fmul2(pq(2), S1)),
+                                            ffma2(NYB, sb, fmul2(pq(3), S1)), fmul2(pq(4), S0),
+                                            fmul2(pq(5), S0)),
+                            NRM);
+                        unpack2(p2, P[i], P[i + 1]);
+                    } else {
+                        const uint64_t p2 = fmul2(
+                            fmul2(std_power2_sums2(NN, NN2, pq(0), pq(1), pq(2), pq(3)), FA),
                             FB);
                         unpack2(p2, P[i], P[i + 1]);
                     }
