@@ -704,8 +704,15 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                         tmem_wait_ld();
                         if (pi) {
 #pragma unroll
-                            for (uint32_t i = 0; i < HALF; ++i)
-                                x[i] = __float_as_uint(__uint_as_float(x[i]) + __uint_as_float(y[i]));
+                            for (uint32_t i = 0; i < HALF; i += 2) {
+                                const uint64_t sum =
+                                    fadd2(pack2(__uint_as_float(x[i]), __uint_as_float(x[i + 1])),
+                                          pack2(__uint_as_float(y[i]), __uint_as_float(y[i + 1])));
+                                float s0f, s1f;
+                                unpack2(sum, s0f, s1f);
+                                x[i] = __float_as_uint(s0f);
+                                x[i + 1] = __float_as_uint(s1f);
+                            }
                         }
                         if (HALF == 32)
                             tmem_st32(run + c, *reinterpret_cast<const uint32_t(*)[32]>(x));
