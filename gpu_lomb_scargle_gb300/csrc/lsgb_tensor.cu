@@ -55,7 +55,7 @@ namespace {
 
 constexpr int kTP = 128;        // fine frequency offsets p: A rows, TMEM lanes
 constexpr int kTK = 16;         // observations per K-block (the FP16 MMA depth)
-constexpr int kPassKB = 4;      // K-blocks accumulated in TMEM before an FP32 fold
+constexpr int kPassKB = 8;      // K-blocks accumulated in TMEM before an FP32 fold
 constexpr int kLoaderWarp = 5;
 constexpr int kProducerWarp0 = 6;
 #ifndef LSGB_TENSOR_PRODUCER_WARPS
