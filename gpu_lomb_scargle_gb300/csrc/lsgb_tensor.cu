@@ -58,12 +58,9 @@ constexpr int kTK = 16;         // observations per K-block (the FP16 MMA depth)
 constexpr int kPassKB = 8;      // K-blocks accumulated in TMEM before an FP32 fold
 constexpr int kLoaderWarp = 5;
 constexpr int kProducerWarp0 = 6;
-#ifndef LSGB_TENSOR_PRODUCER_WARPS
-#define LSGB_TENSOR_PRODUCER_WARPS 4
-#endif
-// 4 producer warps: 14 warps, at most 4 per SM sub-partition, so up to 128 registers per
-// thread; 8: 18 warps and 96 registers
-constexpr int kProducerWarps = LSGB_TENSOR_PRODUCER_WARPS;
+// 14 warps in all, at most 4 per SM sub-partition, so up to 128 registers per thread (8
+// producer warps would make 18 warps and 96 registers, and measured slower)
+constexpr int kProducerWarps = 4;
 constexpr int kProducerThreads = 32 * kProducerWarps;
 constexpr int kEpilogueWarp1 = kProducerWarp0 + kProducerWarps;  // second epilogue group
 constexpr int kThreads = 32 * (kEpilogueWarp1 + 4);
@@ -744,7 +741,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             // quantities: phase 0 groups (re, im) then phase 1 (re, im)
             constexpr int NQ = GEN ? 6 : 4;
             // the standard variant loads chunk m0 + 8 while it computes chunk m0
-            constexpr bool PREFETCH = !GEN && kThreads <= 512;
+            constexpr bool PREFETCH = !GEN;
             uint32_t x[NQ][8];
             auto load_chunk = [&](int m0) {
 #pragma unroll
