@@ -30,16 +30,15 @@
 // the powers from the running sums.
 //
 // One persistent CTA per SM, warp-specialized:
-//   warps 0-3 and the four after the producers: fold and epilogue, two warps per TMEM lane quarter (warp w may
-//               access lanes 32 (w % 4) ..): power per frequency, periodogram store,
-//               per-object maximum;
+//   warps 0-3   fold and epilogue, one warp per TMEM lane quarter (warp w may access lanes
+//               32 (w % 4) ..): power per frequency, periodogram store, per-object maximum;
 //   warp 4      TMEM allocation and the MMA issuer (one thread);
-//   warp 5      operand loader (one thread): bulk copies of the K-block's A matrices from
-//               the operand table into the stage, and L2 prefetches of the table ahead;
-//   warps 6..   producers (kProducerWarps): the split FP16 Z matrix of the stage's K-block,
-//               K-major without swizzle, one sine/cosine per entry, from the K-block's
-//               frequency steps (read from global memory one stage ahead). They start as
-//               soon as the stage is free, in parallel with its bulk copy.
+//   warp 5      operand loader (one thread): bulk copies of a stage's A matrices from the
+//               operand table, and L2 prefetches of the table ahead;
+//   warps 6-13  producers: the split FP16 Z matrices of a stage's K-blocks, K-major without
+//               swizzle, one sine/cosine per entry, from the K-blocks' frequency steps (read
+//               from global memory one K-block ahead). They start as soon as the stage is
+//               free, in parallel with its bulk copy.
 // All hand-offs use mbarriers. Every wait is bounded: on a timeout the kernel records an
 // error in MixedArgs::status, lets its issued MMAs drain, frees its TMEM and returns.
 #include <cuda_fp16.h>
@@ -58,13 +57,16 @@ constexpr int kTK = 16;         // observations per K-block (the FP16 MMA depth)
 constexpr int kPassKB = 8;      // K-blocks accumulated in TMEM before an FP32 fold
 constexpr int kLoaderWarp = 5;
 constexpr int kProducerWarp0 = 6;
-// 14 warps in all, at most 4 per SM sub-partition, so up to 128 registers per thread (8
-// producer warps would make 18 warps and 96 registers, and measured slower)
-constexpr int kProducerWarps = 4;
+// 14 warps in all, at most 4 per SM sub-partition, so up to 128 registers per thread:
+// kEpiPerQuarter epilogue warps per TMEM lane quarter. 1: warps 0-3 and 8 producer warps;
+// 2: warps 0-3 and the four after 4 producer warps (the producers then fall behind the
+// MMA thread: 2-3% slower)
+constexpr int kEpiPerQuarter = 1;
+constexpr int kProducerWarps = kEpiPerQuarter == 2 ? 4 : 8;
 constexpr int kProducerThreads = 32 * kProducerWarps;
 constexpr int kEpilogueWarp1 = kProducerWarp0 + kProducerWarps;  // second epilogue group
-constexpr int kThreads = 32 * (kEpilogueWarp1 + 4);
-constexpr int kEpilogueThreads = 256;  // warps 0-3 and kEpilogueWarp1..+3
+constexpr int kThreads = 32 * (kEpilogueWarp1 + (kEpiPerQuarter == 2 ? 4 : 0));
+constexpr int kEpilogueThreads = 128 * kEpiPerQuarter;
 constexpr uint32_t kPrefetchKB = 32;   // operand-table K-blocks prefetched into L2 ahead
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kBufCols = 128;   // TMEM columns of one partial buffer (two of them)
@@ -654,11 +656,14 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
         __syncwarp();
     } else {
         // ---------------- fold and epilogue ----------------
-        // warp w may access TMEM lanes 32 (w % 4) ..; the two warps of a lane quarter split
-        // the coarse steps: warp half eh owns m in [eh NM/2, (eh+1) NM/2), i.e. the same
-        // half of every NM-column quantity block, in the folds and in the power pass, so a
+        // warp w may access TMEM lanes 32 (w % 4) ..; with two warps per lane quarter they
+        // split the coarse steps: warp half eh owns m in [eh SPAN, (eh+1) SPAN), i.e. the same
+        // part of every NM-column quantity block, in the folds and in the power pass, so a
         // warp only ever reads running sums it wrote itself
-        const uint32_t eq = (uint32_t)warp & 3u, eh = warp >= kEpilogueWarp1 ? 1u : 0u;
+        const uint32_t eq = (uint32_t)warp & 3u;
+        const uint32_t eh = (kEpiPerQuarter == 2 && warp >= kEpilogueWarp1) ? 1u : 0u;
+        // columns of each NM-column quantity block this warp folds and reads: SPAN from eh SPAN
+        constexpr uint32_t SPAN = (uint32_t)G::NM / (uint32_t)kEpiPerQuarter;
         const uint32_t pl = eq * 32u + (uint32_t)lane;
         const uint32_t lane_base = (eq * 32u) << 16;
         const uint32_t run1 = tmem + lane_base + kRun0Col, run2 = tmem + lane_base + kRun1Col;
@@ -683,13 +688,16 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                     }
                     tc_fence_after();
                     const uint32_t part = tmem + lane_base + buf * kBufCols;
-                    // fold: running = (pi ? running : 0) + partial over this warp's half
-                    // of each quantity block; the partial buffer is released as soon as
-                    // both warps of the quarter have read it
-                    constexpr uint32_t HALF = G::NM / 2;
-                    static_assert(HALF == 32 || HALF == 16, "fold rounds of 32 or 16 columns");
+                    // fold: running = (pi ? running : 0) + partial over this warp's part of
+                    // each quantity block; the partial buffer is released as soon as the
+                    // quarter's warps have read it
+                    constexpr uint32_t HALF = SPAN >= 32u ? 32u : 16u;  // columns per round
+                    static_assert(SPAN % HALF == 0, "fold rounds of 32 or 16 columns");
 #pragma unroll 1
-                    for (uint32_t c = HALF * eh; c < wcols; c += G::NM) {
+                    for (uint32_t blk = 0; blk < wcols; blk += G::NM) {  // quantity blocks
+#pragma unroll 1
+                    for (uint32_t cc = 0; cc < SPAN; cc += HALF) {
+                        const uint32_t c = blk + SPAN * eh + cc;
                         uint32_t x[HALF], y[HALF];
                         if (HALF == 32) {
                             tmem_ld32(part + c, *reinterpret_cast<uint32_t(*)[32]>(x));
@@ -715,6 +723,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                             tmem_st32(run + c, *reinterpret_cast<const uint32_t(*)[32]>(x));
                         else
                             tmem_st16(run + c, x);
+                    }
                     }
                     tmem_wait_st();
                     tc_fence_before();
@@ -754,7 +763,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                     tmem_ld8((p1 ? run2 : run1) + col, x[k]);
                 }
             };
-            const int mbeg = (int)eh * (G::NM / 2), mend = mbeg + G::NM / 2;
+            const int mbeg = (int)(eh * SPAN), mend = mbeg + (int)SPAN;
             if (PREFETCH) load_chunk(mbeg);
 #pragma unroll 1
             for (int m0 = mbeg; m0 < mend; m0 += 8) {
