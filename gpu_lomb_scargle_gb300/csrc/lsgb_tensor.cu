@@ -749,9 +749,11 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             if (w.tile == 0 && pl == 0 && eh == 0) bk = 0;  // the reference's (power 0, index 0) start
             // quantities: phase 0 groups (re, im) then phase 1 (re, im)
             constexpr int NQ = GEN ? 6 : 4;
-            // the standard variant loads chunk m0 + 8 while it computes chunk m0
-            constexpr bool PREFETCH = !GEN;
-            uint32_t x[NQ][8];
+            // frequencies per chunk: 16 for the standard variant (eight independent packed
+            // chains per chunk), 8 for the generalized one (six quantities per frequency)
+            constexpr int CHK = GEN ? 8 : 16;
+            static_assert(SPAN % CHK == 0, "whole chunks per warp");
+            uint32_t x[NQ][CHK];
             auto load_chunk = [&](int m0) {
 #pragma unroll
                 for (int k = 0; k < NQ; ++k) {
@@ -760,23 +762,23 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                     // phase 0: group g = kk / 2 of G0, re / im = kk % 2 in [Re groups | Im groups]
                     const uint32_t gq = p1 ? 1u : (uint32_t)G::G0;
                     const uint32_t col = (uint32_t)(kk & 1) * gq * G::NM + (uint32_t)(kk >> 1) * G::NM + (uint32_t)m0;
-                    tmem_ld8((p1 ? run2 : run1) + col, x[k]);
+                    if constexpr (CHK == 16) tmem_ld16((p1 ? run2 : run1) + col, x[k]);
+                    else tmem_ld8((p1 ? run2 : run1) + col, *reinterpret_cast<uint32_t(*)[8]>(x[k]));
                 }
             };
             const int mbeg = (int)(eh * SPAN), mend = mbeg + (int)SPAN;
-            if (PREFETCH) load_chunk(mbeg);
 #pragma unroll 1
-            for (int m0 = mbeg; m0 < mend; m0 += 8) {
-                if (!PREFETCH) load_chunk(m0);
+            for (int m0 = mbeg; m0 < mend; m0 += CHK) {
+                load_chunk(m0);
                 tmem_wait_ld();
-                float q[NQ][8];
+                float q[NQ][CHK];
 #pragma unroll
                 for (int k = 0; k < NQ; ++k)
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) q[k][i] = __uint_as_float(x[k][i]);
-                // the eight powers first, branch-free, so that their chains interleave (the
-                // standard variant in packed pairs of frequencies)
-                float P[8];
+                    for (int i = 0; i < CHK; ++i) q[k][i] = __uint_as_float(x[k][i]);
+                // the chunk's powers first, branch-free and in packed pairs of frequencies, so
+                // that their chains interleave
+                float P[CHK];
                 auto power_at = [&](int i) {
                     if ((i & 1) != 0) return;
                     auto pq = [&](int k) { return pack2(q[k][i], q[k][i + 1]); };
@@ -796,26 +798,22 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                     }
                 };
 #pragma unroll
-                for (int i = 0; i < 4; ++i) power_at(i);
-                // the next chunk's load goes out once half of this chunk's values are dead
-                if (PREFETCH && m0 + 8 < mend) load_chunk(m0 + 8);
-#pragma unroll
-                for (int i = 4; i < 8; ++i) power_at(i);
+                for (int i = 0; i < CHK; ++i) power_at(i);
                 // a thread visits its frequencies in increasing k, so a strictly larger power
                 // is the only way to displace its current best (ties keep the lower index, as
                 // the reference's argmax does)
                 const uint32_t k0 = kT + pl + (uint32_t)kTP * (uint32_t)m0;
-                if (k0 + (uint32_t)kTP * 7u < a.n_freq) {  // the whole chunk is on the grid
+                if (k0 + (uint32_t)kTP * (uint32_t)(CHK - 1) < a.n_freq) {  // the whole chunk is on the grid
                     if (a.pgram) {
 #pragma unroll
-                        for (int i = 0; i < 8; ++i) store_out<OutT>(a.pgram, out0 + k0 + (uint32_t)kTP * (uint32_t)i, P[i]);
+                        for (int i = 0; i < CHK; ++i) store_out<OutT>(a.pgram, out0 + k0 + (uint32_t)kTP * (uint32_t)i, P[i]);
                     }
 #pragma unroll
-                    for (int i = 0; i < 8; ++i)
+                    for (int i = 0; i < CHK; ++i)
                         if (P[i] > bp) { bp = P[i]; bk = k0 + (uint32_t)kTP * (uint32_t)i; }
                 } else {
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) {
+                    for (int i = 0; i < CHK; ++i) {
                         const uint32_t k = k0 + (uint32_t)kTP * (uint32_t)i;
                         if (k < a.n_freq) {
                             if (a.pgram) store_out<OutT>(a.pgram, out0 + k, P[i]);
