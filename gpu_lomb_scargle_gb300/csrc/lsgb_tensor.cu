@@ -32,7 +32,8 @@
 // One persistent CTA per SM, warp-specialized:
 //   warps 0-3   fold and epilogue, one warp per TMEM lane quarter (warp w may access lanes
 //               32 (w % 4) ..): power per frequency, periodogram store, per-object maximum;
-//   warp 4      TMEM allocation and the MMA issuer (one thread);
+//   warp 4      TMEM allocation and the MMA issuer (the whole warp runs the loop, one
+//               elected lane issues);
 //   warp 5      operand loader (one thread): bulk copies of a stage's A matrices from the
 //               operand table, and L2 prefetches of the table ahead;
 //   warps 6-13  producers: the split FP16 Z matrices of a stage's K-blocks, K-major without
@@ -229,26 +230,32 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32
 
 // One complex product's six split-FP16 MMAs into d: a[0..3] = (re hi, re lo, im hi, im lo),
 // b[0..3] = (window [Br; Bi] hi, lo, window [-Bi; Br] hi, lo); the first MMA overwrites d
-// unless `accumulate`.
+// unless `accumulate`. Called by a whole converged warp: elect.sync picks the one lane that
+// issues, so the warp's loop stays uniform and its descriptors need no per-lane moves.
 __device__ __forceinline__ void mma_cplx6(uint32_t d, const uint64_t (&a)[4],
                                           const uint64_t (&b)[4], uint32_t idesc,
                                           uint32_t accumulate) {
     asm volatile(
-        "{ .reg .pred p0, pt; setp.ne.b32 p0, %9, 0; setp.eq.b32 pt, %9, %9;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %5, %10, p0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %6, %10, pt;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %2, %5, %10, pt;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %3, %7, %10, pt;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %3, %8, %10, pt;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %4, %7, %10, pt; }" ::"r"(d),
+        "{ .reg .pred p0, pt, e; elect.sync _|e, 0xffffffff;\n\t"
+        "setp.ne.b32 p0, %9, 0; setp.eq.b32 pt, %9, %9;\n\t"
+        "@e tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %5, %10, p0;\n\t"
+        "@e tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %6, %10, pt;\n\t"
+        "@e tcgen05.mma.cta_group::1.kind::f16 [%0], %2, %5, %10, pt;\n\t"
+        "@e tcgen05.mma.cta_group::1.kind::f16 [%0], %3, %7, %10, pt;\n\t"
+        "@e tcgen05.mma.cta_group::1.kind::f16 [%0], %3, %8, %10, pt;\n\t"
+        "@e tcgen05.mma.cta_group::1.kind::f16 [%0], %4, %7, %10, pt; }" ::"r"(d),
         "l"(a[0]), "l"(a[1]), "l"(a[2]), "l"(a[3]), "l"(b[0]), "l"(b[1]), "l"(b[2]), "l"(b[3]),
         "r"(accumulate), "r"(idesc)
         : "memory");
 }
+// Arrives on b once every MMA issued so far has completed (whole converged warp, one lane
+// commits).
 __device__ __forceinline__ void mma_commit(uint64_t *b) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                     smem_u32(b))
-                 : "memory");
+    asm volatile(
+        "{ .reg .pred e; elect.sync _|e, 0xffffffff;\n\t"
+        "@e tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0]; }" ::"r"(
+            smem_u32(b))
+        : "memory");
 }
 __device__ __forceinline__ void tc_fence_after() {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -581,7 +588,9 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
         __syncwarp();
     } else if (warp == 4) {
         // ---------------- MMA issuer ----------------
-        if (lane == 0) {
+        // The whole warp walks the loop (every value in it is warp-uniform and every wait
+        // ends in a vote); one elected lane issues the MMAs and commits.
+        {
             constexpr uint32_t idesc0 = idesc_f16(kTP, G::N0), idesc1 = idesc_f16(kTP, G::N1);
             // descriptors: the upper 32 bits are the same for every operand; the address
             // field of the lower ones is linear in the shared address (16-byte units; shared
@@ -600,7 +609,8 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                 for (uint32_t ph = 0; ph < 2 && ok; ++ph) {
                     for (uint32_t kb0 = 0; kb0 < w.nkb && ok; kb0 += kPassKB, ++gp) {
                         const uint32_t buf = gp & 1u, ub = gp >> 1;
-                        if (!mbar_wait(&pempty_bar[buf], (ub & 1u) ^ 1u, &s_abort, a.status)) {
+                        if (!__all_sync(0xffffffffu, mbar_wait(&pempty_bar[buf], (ub & 1u) ^ 1u,
+                                                               &s_abort, a.status))) {
                             ok = false;
                             break;
                         }
@@ -613,7 +623,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                         const uint32_t wre = gnm * (uint32_t)G::NM * 32u;
                         const uint32_t idesc = ph ? idesc1 : idesc0;
                         for (uint32_t kb = kb0; kb < kb1; kb += G::KPS) {  // one stage
-                            if (!mbar_wait(&full_bar[s], sph, &s_abort, a.status)) {
+                            if (!__all_sync(0xffffffffu, mbar_wait(&full_bar[s], sph, &s_abort, a.status))) {
                                 ok = false;
                                 break;
                             }
