@@ -230,19 +230,21 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32
 
 // One complex product's six split-FP16 MMAs into d: a[0..3] = (re hi, re lo, im hi, im lo),
 // b[0..3] = (window [Br; Bi] hi, lo, window [-Bi; Br] hi, lo); the first MMA overwrites d
-// unless `accumulate`. Called by a whole converged warp: elect.sync picks the one lane that
-// issues, so the warp's loop stays uniform and its descriptors need no per-lane moves.
+// unless `accumulate`. The two MMAs that share an A matrix read it once: the first fills
+// the A collector buffer, the second takes it from there. Called by a whole converged warp:
+// elect.sync picks the one lane that issues, so the warp's loop stays uniform and its
+// descriptors need no per-lane moves.
 __device__ __forceinline__ void mma_cplx6(uint32_t d, const uint64_t (&a)[4],
                                           const uint64_t (&b)[4], uint32_t idesc,
                                           uint32_t accumulate) {
     asm volatile(
         "{ .reg .pred p0, pt, e; elect.sync _|e, 0xffffffff;\n\t"
         "setp.ne.b32 p0, %9, 0; setp.eq.b32 pt, %9, %9;\n\t"
-        "@e tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %5, %10, p0;\n\t"
-        "@e tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %6, %10, pt;\n\t"
+        "@e tcgen05.mma.cta_group::1.kind::f16.collector::a::fill [%0], %1, %5, %10, p0;\n\t"
+        "@e tcgen05.mma.cta_group::1.kind::f16.collector::a::lastuse [%0], %1, %6, %10, pt;\n\t"
         "@e tcgen05.mma.cta_group::1.kind::f16 [%0], %2, %5, %10, pt;\n\t"
-        "@e tcgen05.mma.cta_group::1.kind::f16 [%0], %3, %7, %10, pt;\n\t"
-        "@e tcgen05.mma.cta_group::1.kind::f16 [%0], %3, %8, %10, pt;\n\t"
+        "@e tcgen05.mma.cta_group::1.kind::f16.collector::a::fill [%0], %3, %7, %10, pt;\n\t"
+        "@e tcgen05.mma.cta_group::1.kind::f16.collector::a::lastuse [%0], %3, %8, %10, pt;\n\t"
         "@e tcgen05.mma.cta_group::1.kind::f16 [%0], %4, %7, %10, pt; }" ::"r"(d),
         "l"(a[0]), "l"(a[1]), "l"(a[2]), "l"(a[3]), "l"(b[0]), "l"(b[1]), "l"(b[2]), "l"(b[3]),
         "r"(accumulate), "r"(idesc)
