@@ -24,10 +24,11 @@
 //
 // The tensor cores round their FP32 accumulations toward zero, which makes the error of
 // a long accumulation grow linearly with its length. So a unit's observations are summed
-// in passes of kPassKB K-blocks into one of two TMEM partial buffers, and the epilogue
-// warps fold each finished pass into an FP32 running sum in TMEM with round-to-nearest
-// adds, releasing the partial buffer at once; after the last pass of a unit they compute
-// the powers from the running sums.
+// in passes of kPassKB K-blocks. TMEM holds four slots of accumulators: a phase's first
+// pass accumulates into a free slot, which then holds that phase's running sum; each later
+// pass accumulates into another free slot, which the epilogue warps fold into the running
+// sum with round-to-nearest adds and free at once; after the last pass of a unit they
+// compute the powers from the two running sums and free their slots (SlotRing).
 //
 // One persistent CTA per SM, warp-specialized:
 //   warps 0-3   fold and epilogue, one warp per TMEM lane quarter (warp w may access lanes
@@ -70,9 +71,8 @@ constexpr int kThreads = 32 * (kEpilogueWarp1 + (kEpiPerQuarter == 2 ? 4 : 0));
 constexpr int kEpilogueThreads = 128 * kEpiPerQuarter;
 constexpr uint32_t kPrefetchKB = 32;   // operand-table K-blocks prefetched into L2 ahead
 constexpr uint32_t kTmemCols = 512;
-constexpr uint32_t kBufCols = 128;   // TMEM columns of one partial buffer (two of them)
-constexpr uint32_t kRun0Col = 256;   // running sums of phase 0 (exp(i theta) sums)
-constexpr uint32_t kRun1Col = 384;   // running sums of phase 1 (exp(2i theta) sums)
+constexpr uint32_t kSlots = 4;       // TMEM accumulator slots
+constexpr uint32_t kSlotCols = 128;  // TMEM columns of one slot
 constexpr long long kWaitCycles = 1ll << 32;  // ~2 s at 2 GHz
 
 // Per-variant geometry.
@@ -109,8 +109,8 @@ struct TGeo {
     // observations in JS slices
     static constexpr int JPT = NM * kTK / kProducerThreads;
     static constexpr int JS = kTK / JPT;
-    static_assert(W0 <= (int)kBufCols && W1 <= (int)kBufCols, "partial buffer too narrow");
-    static_assert(kRun1Col + W1 <= kTmemCols && kRun0Col + W0 <= kRun1Col, "TMEM layout");
+    static_assert(W0 <= (int)kSlotCols && W1 <= (int)kSlotCols, "TMEM slot too narrow");
+    static_assert(kSlots * kSlotCols == kTmemCols, "TMEM layout");
     static_assert(NM % 32 == 0 && (JPT == 2 || JPT == 4 || JPT == 8), "producer mapping");
     static_assert(NM * kTK == kProducerThreads * JPT, "one Z entry per producer and observation");
 };
@@ -367,6 +367,32 @@ struct UnitWalk {
     }
 };
 
+// Which TMEM slot each pass accumulates into. Free slots are handed out in the order they
+// were freed: pop() for every pass in order; a phase's first pass keeps its slot as the
+// running sum, a later pass's slot is pushed back once the epilogue has folded it, and the
+// unit's two running-sum slots are pushed back after its power pass. The MMA warp and the
+// epilogue warps run this same bookkeeping over the same sequence of passes, so they agree
+// on every pass's slot without exchanging it. At most two slots are held across a pass
+// boundary (the running sums), so a pop always finds one; the slot's barriers alternate
+// between its full and empty phases, whose parity is the count of its uses so far.
+struct SlotRing {
+    uint32_t q = 0xE4u;  // queued free slots, 2 bits each, head in the low bits: 0, 1, 2, 3
+    uint32_t n = kSlots;
+    uint32_t par = 0u;   // bit s: parity of slot s's uses before the current one
+    __device__ __forceinline__ uint32_t pop(uint32_t &parity) {
+        const uint32_t s = q & 3u;
+        q >>= 2;
+        --n;
+        parity = (par >> s) & 1u;
+        par ^= 1u << s;
+        return s;
+    }
+    __device__ __forceinline__ void push(uint32_t s) {
+        q |= s << (2u * n);
+        ++n;
+    }
+};
+
 template <bool GEN, typename OutT>
 __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
     using G = TGeo<GEN>;
@@ -378,7 +404,9 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
     // matrix is written (the producers' arrivals); empty: its MMAs have completed (the
     // loader and the producers wait for it)
     __shared__ __align__(8) uint64_t full_bar[S], empty_bar[S];
-    __shared__ __align__(8) uint64_t pfull_bar[2], pempty_bar[2], drain_bar;
+    // sfull: a pass's MMAs into the slot have completed; sempty: the epilogue has folded the
+    // slot or, for a running sum, finished the unit's power pass
+    __shared__ __align__(8) uint64_t sfull_bar[kSlots], sempty_bar[kSlots], drain_bar;
     __shared__ uint32_t s_tmem;
     __shared__ volatile uint32_t s_abort;
 
@@ -390,9 +418,9 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             mbar_init(&full_bar[s], kProducerWarps + 1);  // one arrival per producer warp
             mbar_init(&empty_bar[s], 1);
         }
-        for (int b = 0; b < 2; ++b) {
-            mbar_init(&pfull_bar[b], 1);
-            mbar_init(&pempty_bar[b], kEpilogueThreads / 32);  // one arrival per warp
+        for (uint32_t b = 0; b < kSlots; ++b) {
+            mbar_init(&sfull_bar[b], 1);
+            mbar_init(&sempty_bar[b], kEpilogueThreads / 32);  // one arrival per warp
         }
         mbar_init(&drain_bar, 1);
         s_abort = 0u;
@@ -602,22 +630,25 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             auto dsc = [&](uint32_t lo, uint32_t off) -> uint64_t {
                 return ((uint64_t)dhi << 32) | (uint64_t)(lo + (off >> 4));
             };
-            uint32_t s = 0, sph = 0, gp = 0;  // stage slot and its phase parity; pass count
-            uint32_t dlo = dlo0;              // lower descriptor half of slot s
+            uint32_t s = 0, sph = 0;  // stage slot and its phase parity
+            uint32_t dlo = dlo0;      // lower descriptor half of slot s
             bool ok = true;
+            SlotRing ring;
+            uint32_t rsum[2] = {0u, 0u};  // the unit's running-sum slots
             UnitWalk walk(a, units);
             for (uint32_t u = blockIdx.x; u < units && ok; u += gridDim.x) {
-                const UnitInfo w = walk.next(a, u, units);
+                const UnitInfo w = walk.next(a, u, units);  // nkb >= 1: no object is empty
                 for (uint32_t ph = 0; ph < 2 && ok; ++ph) {
-                    for (uint32_t kb0 = 0; kb0 < w.nkb && ok; kb0 += kPassKB, ++gp) {
-                        const uint32_t buf = gp & 1u, ub = gp >> 1;
-                        if (!__all_sync(0xffffffffu, mbar_wait(&pempty_bar[buf], (ub & 1u) ^ 1u,
+                    for (uint32_t kb0 = 0; kb0 < w.nkb && ok; kb0 += kPassKB) {
+                        uint32_t sp;
+                        const uint32_t slot = ring.pop(sp);
+                        if (!__all_sync(0xffffffffu, mbar_wait(&sempty_bar[slot], sp ^ 1u,
                                                                &s_abort, a.status))) {
                             ok = false;
                             break;
                         }
                         tc_fence_after();
-                        const uint32_t d0 = tmem + buf * kBufCols;
+                        const uint32_t d0 = tmem + slot * kSlotCols;
                         const uint32_t kb1 = min(w.nkb, kb0 + (uint32_t)kPassKB);
                         // windows of Z = [-Bi; Br; Bi] (blocks of G NM rows): [Br; Bi] at
                         // row G NM, [-Bi; Br] at row 0
@@ -655,9 +686,14 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                                 dlo += (uint32_t)G::STAGE >> 4;
                             }
                         }
-                        if (ok) mma_commit(&pfull_bar[buf]);
+                        if (ok) mma_commit(&sfull_bar[slot]);
+                        // the epilogue's side of the bookkeeping
+                        if (kb0 == 0) rsum[ph] = slot;
+                        else ring.push(slot);
                     }
                 }
+                ring.push(rsum[0]);
+                ring.push(rsum[1]);
             }
             // every issued MMA has completed before TMEM is released
             mma_commit(&drain_bar);
@@ -678,9 +714,8 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
         constexpr uint32_t SPAN = (uint32_t)G::NM / (uint32_t)kEpiPerQuarter;
         const uint32_t pl = eq * 32u + (uint32_t)lane;
         const uint32_t lane_base = (eq * 32u) << 16;
-        const uint32_t run1 = tmem + lane_base + kRun0Col, run2 = tmem + lane_base + kRun1Col;
-        uint32_t gp = 0;
         bool ok = true;
+        SlotRing ring;
         UnitWalk walk(a, units);
         for (uint32_t u = blockIdx.x; u < units && ok; u += gridDim.x) {
             const UnitInfo w = walk.next(a, u, units);
@@ -689,20 +724,26 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             const float nrm = ob.norm32, tsc0 = ob.tsc0, tsc1 = ob.tsc1;
             const float invw = ob.invw32, ybar = ob.ybar32;
             const uint32_t npass = (w.nkb + kPassKB - 1) / kPassKB;
+            uint32_t rsum[2] = {0u, 0u};  // the running-sum slots of the two phases
             for (uint32_t ph = 0; ph < 2 && ok; ++ph) {
-                const uint32_t run = ph ? run2 : run1;
                 const uint32_t wcols = ph ? (uint32_t)G::W1 : (uint32_t)G::W0;
-                for (uint32_t pi = 0; pi < npass; ++pi, ++gp) {
-                    const uint32_t buf = gp & 1u, ub = gp >> 1;
-                    if (!__all_sync(0xffffffffu, mbar_wait(&pfull_bar[buf], ub & 1u, &s_abort, a.status))) {
+                for (uint32_t pi = 0; pi < npass; ++pi) {
+                    uint32_t sp;
+                    const uint32_t slot = ring.pop(sp);
+                    if (!__all_sync(0xffffffffu, mbar_wait(&sfull_bar[slot], sp, &s_abort, a.status))) {
                         ok = false;
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t part = tmem + lane_base + buf * kBufCols;
-                    // fold: running = (pi ? running : 0) + partial over this warp's part of
-                    // each quantity block; the partial buffer is released as soon as the
-                    // quarter's warps have read it
+                    // the first pass's slot becomes the running sum as it is
+                    if (pi == 0) {
+                        rsum[ph] = slot;
+                        continue;
+                    }
+                    const uint32_t run = tmem + lane_base + rsum[ph] * kSlotCols;
+                    const uint32_t part = tmem + lane_base + slot * kSlotCols;
+                    // fold: running += partial over this warp's part of each quantity block;
+                    // the slot is freed as soon as the quarter's warps have read it
                     constexpr uint32_t HALF = SPAN >= 32u ? 32u : 16u;  // columns per round
                     static_assert(SPAN % HALF == 0, "fold rounds of 32 or 16 columns");
 #pragma unroll 1
@@ -713,23 +754,21 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                         uint32_t x[HALF], y[HALF];
                         if (HALF == 32) {
                             tmem_ld32(part + c, *reinterpret_cast<uint32_t(*)[32]>(x));
-                            if (pi) tmem_ld32(run + c, *reinterpret_cast<uint32_t(*)[32]>(y));
+                            tmem_ld32(run + c, *reinterpret_cast<uint32_t(*)[32]>(y));
                         } else {
                             tmem_ld16(part + c, x);
-                            if (pi) tmem_ld16(run + c, y);
+                            tmem_ld16(run + c, y);
                         }
                         tmem_wait_ld();
-                        if (pi) {
 #pragma unroll
-                            for (uint32_t i = 0; i < HALF; i += 2) {
-                                const uint64_t sum =
-                                    fadd2(pack2(__uint_as_float(x[i]), __uint_as_float(x[i + 1])),
-                                          pack2(__uint_as_float(y[i]), __uint_as_float(y[i + 1])));
-                                float s0f, s1f;
-                                unpack2(sum, s0f, s1f);
-                                x[i] = __float_as_uint(s0f);
-                                x[i + 1] = __float_as_uint(s1f);
-                            }
+                        for (uint32_t i = 0; i < HALF; i += 2) {
+                            const uint64_t sum =
+                                fadd2(pack2(__uint_as_float(x[i]), __uint_as_float(x[i + 1])),
+                                      pack2(__uint_as_float(y[i]), __uint_as_float(y[i + 1])));
+                            float s0f, s1f;
+                            unpack2(sum, s0f, s1f);
+                            x[i] = __float_as_uint(s0f);
+                            x[i + 1] = __float_as_uint(s1f);
                         }
                         if (HALF == 32)
                             tmem_st32(run + c, *reinterpret_cast<const uint32_t(*)[32]>(x));
@@ -740,11 +779,14 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                     tmem_wait_st();
                     tc_fence_before();
                     __syncwarp();
-                    if (lane == 0) mbar_arrive(&pempty_bar[buf]);
+                    if (lane == 0) mbar_arrive(&sempty_bar[slot]);
+                    ring.push(slot);
                 }
             }
             if (!ok) break;
             // power from the running sums of both phases
+            const uint32_t run1 = tmem + lane_base + rsum[0] * kSlotCols;
+            const uint32_t run2 = tmem + lane_base + rsum[1] * kSlotCols;
             const uint32_t kT = w.tile * (uint32_t)G::TILE;
             const float us0 = 1.0f / tsc0, us1 = 1.0f / tsc1;  // powers of two
             // standard: P = (2P of the raw sums) us0 (us0 nrm / 2), the scale applied in
@@ -834,6 +876,15 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                     }
                 }
             }
+            // every load of the running sums has completed: free their slots
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(&sempty_bar[rsum[0]]);
+                mbar_arrive(&sempty_bar[rsum[1]]);
+            }
+            ring.push(rsum[0]);
+            ring.push(rsum[1]);
             if (a.best_key) {
 #pragma unroll
                 for (int off = 16; off > 0; off >>= 1) {
