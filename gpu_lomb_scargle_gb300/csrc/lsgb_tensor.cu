@@ -39,8 +39,9 @@
 //               operand table, and L2 prefetches of the table ahead;
 //   warps 6-13  producers: the split FP16 Z matrices of a stage's K-blocks, K-major without
 //               swizzle, one sine/cosine per entry, from the K-blocks' frequency steps (read
-//               from global memory one K-block ahead). They start as soon as the stage is
-//               free, in parallel with its bulk copy.
+//               from global memory one stage ahead); warps 6-9 build a stage's first K-block,
+//               warps 10-13 its second. They start as soon as the stage is free, in parallel
+//               with its bulk copy.
 // All hand-offs use mbarriers. Every wait is bounded: on a timeout the kernel records an
 // error in MixedArgs::status, lets its issued MMAs drain, frees its TMEM and returns.
 #include <cuda_fp16.h>
@@ -62,10 +63,9 @@ constexpr int kProducerWarp0 = 6;
 // 14 warps in all, at most 4 per SM sub-partition, so up to 128 registers per thread:
 // kEpiPerQuarter epilogue warps per TMEM lane quarter. 1: warps 0-3 and 8 producer warps;
 // 2: warps 0-3 and the four after 4 producer warps (the producers then fall behind the
-// MMA thread: 2-3% slower)
+// MMA warp: 2-3% slower)
 constexpr int kEpiPerQuarter = 1;
 constexpr int kProducerWarps = kEpiPerQuarter == 2 ? 4 : 8;
-constexpr int kProducerThreads = 32 * kProducerWarps;
 constexpr int kEpilogueWarp1 = kProducerWarp0 + kProducerWarps;  // second epilogue group
 constexpr int kThreads = 32 * (kEpilogueWarp1 + (kEpiPerQuarter == 2 ? 4 : 0));
 constexpr int kEpilogueThreads = 128 * kEpiPerQuarter;
@@ -105,14 +105,9 @@ struct TGeo {
     // bytes per observation of the steps array: b (standard), b and the two scaled
     // weights (generalized)
     static constexpr int SB = GEN ? 16 : 8;
-    // producers: one row m and JPT consecutive observations per thread; the K-block's 16
-    // observations in JS slices
-    static constexpr int JPT = NM * kTK / kProducerThreads;
-    static constexpr int JS = kTK / JPT;
     static_assert(W0 <= (int)kSlotCols && W1 <= (int)kSlotCols, "TMEM slot too narrow");
     static_assert(kSlots * kSlotCols == kTmemCols, "TMEM layout");
-    static_assert(NM % 32 == 0 && (JPT == 2 || JPT == 4 || JPT == 8), "producer mapping");
-    static_assert(NM * kTK == kProducerThreads * JPT, "one Z entry per producer and observation");
+    static_assert(NM % 32 == 0 && kProducerWarps % KPS == 0, "producer mapping");
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -444,21 +439,28 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
     if (warp >= kProducerWarp0 && warp < kEpilogueWarp1) {
         // ---------------- producers ----------------
         // Z entry (m, j): B = exp(i (kT + 128 m) b_j) (phase 0) or its square (phase 1).
-        // A thread owns row m and the JPT observations j0.. of the K-block: one 2 JPT-byte
+        // The producer warps come in KPS groups, group hk building K-block hk of every stage.
+        // A thread owns row m and the JPT observations j0.. of its K-block: one 2 JPT-byte
         // store per row kind (-Bi, Br, Bi) and half (hi, lo). The lanes of a quarter-warp
         // own 8 consecutive rows of one core matrix, so the stores have no bank conflicts.
-        constexpr uint32_t JPT = (uint32_t)G::JPT, JS = (uint32_t)G::JS;
-        // quarter-warp c of the producers: observation slice c % JS, row group c / JS
-        const uint32_t c = ((uint32_t)lane >> 3) + 4u * (uint32_t)(warp - kProducerWarp0);
+        constexpr uint32_t GW = (uint32_t)kProducerWarps / (uint32_t)G::KPS;  // warps a group
+        constexpr uint32_t JPT = (uint32_t)G::NM * kTK / (32u * GW);
+        constexpr uint32_t JS = kTK / JPT;
+        static_assert(JPT == 4 || JPT == 8, "producer mapping");
+        const uint32_t pw = (uint32_t)(warp - kProducerWarp0);
+        const uint32_t hk = pw / GW;
+        // quarter-warp c of the group: observation slice c % JS, row group c / JS
+        const uint32_t c = ((uint32_t)lane >> 3) + 4u * (pw % GW);
         const uint32_t m = 8u * (c / JS) + ((uint32_t)lane & 7u);
         const uint32_t j0 = JPT * (c % JS);
         // group g of G: rows g NM + m (-Bi), (G + g) NM + m (Br), (2G + g) NM + m (Bi) of the
         // hi matrix; lo is Z_BYTES further
-        const uint32_t zo = (uint32_t)G::Z_OFF + kmaj_off(m, j0);
+        const uint32_t zo = (uint32_t)G::Z_OFF + hk * (uint32_t)G::ZKB + kmaj_off(m, j0);
         constexpr uint32_t kRowNM = (uint32_t)G::NM * 32u;  // kmaj_off(r + NM) - kmaj_off(r)
         uint32_t g = 0;
         UnitWalk walk(a, units);
-        // the steps (and weights) of the next stage's K-block, loaded one stage ahead
+        // the steps (and weights) of the group's K-block of the next stage, loaded one stage
+        // ahead (only for K-blocks that exist)
         constexpr uint32_t NQ4 = JPT * (uint32_t)G::SB / 16u;  // uint4 per thread and stage
         const uint4 *steps = static_cast<const uint4 *>(a.steps);
         uint4 nb[NQ4];
@@ -467,115 +469,114 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             for (uint32_t h = 0; h < NQ4; ++h)
                 nb[h] = __ldg(steps + (kbg * kTK + j0) * (uint32_t)G::SB / 16u + h);
         };
-        if (blockIdx.x < units) load_b(walk.nxt.kb0);
+        if (blockIdx.x < units && hk < walk.nxt.nkb) load_b(walk.nxt.kb0 + hk);
         // the warp's lanes leave together: the abort flag as lane 0 reads it, and every
         // wait's outcome voted over the warp
         for (uint32_t u = blockIdx.x; u < units && __shfl_sync(0xffffffffu, s_abort, 0) == 0u;
              u += gridDim.x) {
             const UnitInfo w = walk.next(a, u, units);
             const uint32_t k = w.tile * (uint32_t)G::TILE + 128u * m;
-            uint32_t s = 0;
-            for (uint32_t ks = 0; ks < 2u * w.nkb; ++ks) {
-                const bool ph1 = ks >= w.nkb;
-                const uint32_t kb = ph1 ? ks - w.nkb : ks;
-                const uint32_t kbi = kb % (uint32_t)G::KPS;  // K-block within the stage
-                const bool last = kbi == (uint32_t)G::KPS - 1u || kb + 1u == w.nkb;
+            const uint32_t nsp = (w.nkb + (uint32_t)G::KPS - 1u) / (uint32_t)G::KPS;  // a phase
+            bool ok = true;
+            for (uint32_t st = 0; st < 2u * nsp; ++st) {
+                const bool ph1 = st >= nsp;
+                const uint32_t kb = (ph1 ? st - nsp : st) * (uint32_t)G::KPS + hk;
+                const bool mine = kb < w.nkb;
                 uint4 cb[NQ4];
 #pragma unroll
                 for (uint32_t h = 0; h < NQ4; ++h) cb[h] = nb[h];
-                const uint32_t ks1 = ks + 1u;
-                if (ks1 < 2u * w.nkb)
-                    load_b(w.kb0 + (ks1 < w.nkb ? ks1 : ks1 - w.nkb));
-                else if (u + gridDim.x < units)
-                    load_b(walk.nxt.kb0);
-                if (kbi == 0u) {  // a new stage
-                    s = g % S;
-                    const uint32_t us = g / S;
-                    if (!__all_sync(0xffffffffu,
-                                    mbar_wait(&empty_bar[s], (us & 1u) ^ 1u, &s_abort, a.status)))
-                        break;
-                }
-                unsigned char *zh = ring + (size_t)s * G::STAGE + zo + kbi * (uint32_t)G::ZKB;
-                auto put = [&](unsigned char *dst, const uint32_t (&v)[JPT / 2]) {
-                    if constexpr (JPT == 8)
-                        *reinterpret_cast<uint4 *>(dst) = make_uint4(v[0], v[1], v[2], v[3]);
-                    else if constexpr (JPT == 4)
-                        *reinterpret_cast<uint2 *>(dst) = make_uint2(v[0], v[1]);
-                    else
-                        *reinterpret_cast<uint32_t *>(dst) = v[0];
-                };
-                // the observations in pairs (j, j + 1): cos / sin of k b_j (or of twice it),
-                // times the group weights, split and packed as FP16 pairs
-                const uint32_t ng = (GEN && !ph1) ? 2u : 1u;
-                uint32_t pch[2][JPT / 2], pcl[2][JPT / 2], psh[2][JPT / 2], psl[2][JPT / 2];
-#pragma unroll
-                for (uint32_t h = 0; h < JPT / 2; ++h) {
-                    uint32_t bl[2], bh[2];
-                    float wt[2][2];  // [observation][group]
-                    if constexpr (GEN) {
-                        const uint4 q0 = cb[2 * h], q1 = cb[2 * h + 1];
-                        bl[0] = q0.x; bh[0] = q0.y; bl[1] = q1.x; bh[1] = q1.y;
-                        wt[0][0] = __uint_as_float(q0.z); wt[0][1] = __uint_as_float(q0.w);
-                        wt[1][0] = __uint_as_float(q1.z); wt[1][1] = __uint_as_float(q1.w);
-                    } else {
-                        bl[0] = cb[h].x; bh[0] = cb[h].y; bl[1] = cb[h].z; bh[1] = cb[h].w;
-                        wt[0][0] = wt[0][1] = wt[1][0] = wt[1][1] = 1.0f;
-                    }
-                    float sn[2], cs[2];
-#pragma unroll
-                    for (int q = 0; q < 2; ++q) {
-                        // hi 32 bits of k b mod 2^64: (k b_lo) >> 32 plus k b_hi
-                        const uint32_t t32 = __umulhi(k, bl[q]) + k * bh[q];
-                        turn_sincos(t32, sn[q], cs[q]);
-                    }
-                    // the two observations as packed pairs; the doubled angle of phase 1
-                    uint64_t C = pack2(cs[0], cs[1]), Sn = pack2(sn[0], sn[1]);
-                    if (ph1) {
-                        const uint64_t C2 = fsub2(fmul2(C, C), fmul2(Sn, Sn));
-                        Sn = fmul2(fadd2(C, C), Sn);
-                        C = C2;
-                    }
-#pragma unroll
-                    for (int gi = 0; gi < (GEN ? 2 : 1); ++gi) {
-                        if (gi >= (int)ng) break;  // phase 1 has one group
-                        uint64_t Cg = C, Sg = Sn;
-                        if (GEN) {
-                            const uint64_t W = pack2(wt[0][gi], wt[1][gi]);
-                            Cg = fmul2(C, W);
-                            Sg = fmul2(Sn, W);
-                        }
-                        split2(Cg, pch[gi][h], pcl[gi][h]);
-                        split2(Sg, psh[gi][h], psl[gi][h]);
+                // the group's K-block of the next stage: this unit's, or the next unit's first
+                {
+                    const uint32_t st1 = st + 1u;
+                    if (st1 < 2u * nsp) {
+                        const uint32_t kb1 = (st1 >= nsp ? st1 - nsp : st1) * (uint32_t)G::KPS + hk;
+                        if (kb1 < w.nkb) load_b(w.kb0 + kb1);
+                    } else if (u + gridDim.x < units && hk < walk.nxt.nkb) {
+                        load_b(walk.nxt.kb0 + hk);
                     }
                 }
-#pragma unroll
-                for (uint32_t gi = 0; gi < (GEN ? 2u : 1u); ++gi) {
-                    if (gi >= ng) break;
-                    // -x = (-hi) + (-lo) exactly: the sign bits of both FP16 halves flipped
-                    uint32_t nsh[JPT / 2], nsl[JPT / 2];
+                const uint32_t s = g % S, us = g / S;
+                if (!__all_sync(0xffffffffu,
+                                mbar_wait(&empty_bar[s], (us & 1u) ^ 1u, &s_abort, a.status))) {
+                    ok = false;
+                    break;
+                }
+                if (mine) {
+                    unsigned char *zh = ring + (size_t)s * G::STAGE + zo;
+                    auto put = [&](unsigned char *dst, const uint32_t (&v)[JPT / 2]) {
+                        if constexpr (JPT == 8)
+                            *reinterpret_cast<uint4 *>(dst) = make_uint4(v[0], v[1], v[2], v[3]);
+                        else
+                            *reinterpret_cast<uint2 *>(dst) = make_uint2(v[0], v[1]);
+                    };
+                    // the observations in pairs (j, j + 1): cos / sin of k b_j (or of twice
+                    // it), times the group weights, split and packed as FP16 pairs
+                    const uint32_t ng = (GEN && !ph1) ? 2u : 1u;
+                    uint32_t pch[2][JPT / 2], pcl[2][JPT / 2], psh[2][JPT / 2], psl[2][JPT / 2];
 #pragma unroll
                     for (uint32_t h = 0; h < JPT / 2; ++h) {
-                        nsh[h] = psh[gi][h] ^ 0x80008000u;
-                        nsl[h] = psl[gi][h] ^ 0x80008000u;
+                        uint32_t bl[2], bh[2];
+                        float wt[2][2];  // [observation][group]
+                        if constexpr (GEN) {
+                            const uint4 q0 = cb[2 * h], q1 = cb[2 * h + 1];
+                            bl[0] = q0.x; bh[0] = q0.y; bl[1] = q1.x; bh[1] = q1.y;
+                            wt[0][0] = __uint_as_float(q0.z); wt[0][1] = __uint_as_float(q0.w);
+                            wt[1][0] = __uint_as_float(q1.z); wt[1][1] = __uint_as_float(q1.w);
+                        } else {
+                            bl[0] = cb[h].x; bh[0] = cb[h].y; bl[1] = cb[h].z; bh[1] = cb[h].w;
+                            wt[0][0] = wt[0][1] = wt[1][0] = wt[1][1] = 1.0f;
+                        }
+                        float sn[2], cs[2];
+#pragma unroll
+                        for (int q = 0; q < 2; ++q) {
+                            // hi 32 bits of k b mod 2^64: (k b_lo) >> 32 plus k b_hi
+                            const uint32_t t32 = __umulhi(k, bl[q]) + k * bh[q];
+                            // phase 1: the doubled angle is the doubled turn count (mod 2^32)
+                            turn_sincos(ph1 ? t32 << 1 : t32, sn[q], cs[q]);
+                        }
+                        // the two observations as packed pairs
+                        const uint64_t C = pack2(cs[0], cs[1]), Sn = pack2(sn[0], sn[1]);
+#pragma unroll
+                        for (int gi = 0; gi < (GEN ? 2 : 1); ++gi) {
+                            if (gi >= (int)ng) break;  // phase 1 has one group
+                            uint64_t Cg = C, Sg = Sn;
+                            if (GEN) {
+                                const uint64_t W = pack2(wt[0][gi], wt[1][gi]);
+                                Cg = fmul2(C, W);
+                                Sg = fmul2(Sn, W);
+                            }
+                            split2(Cg, pch[gi][h], pcl[gi][h]);
+                            split2(Sg, psh[gi][h], psl[gi][h]);
+                        }
                     }
-                    unsigned char *zg = zh + gi * kRowNM;
-                    put(zg, nsh);
-                    put(zg + G::Z_BYTES, nsl);
-                    put(zg + ng * kRowNM, pch[gi]);
-                    put(zg + ng * kRowNM + G::Z_BYTES, pcl[gi]);
-                    put(zg + 2u * ng * kRowNM, psh[gi]);
-                    put(zg + 2u * ng * kRowNM + G::Z_BYTES, psl[gi]);
+#pragma unroll
+                    for (uint32_t gi = 0; gi < (GEN ? 2u : 1u); ++gi) {
+                        if (gi >= ng) break;
+                        // -x = (-hi) + (-lo) exactly: the sign bits of both FP16 halves flipped
+                        uint32_t nsh[JPT / 2], nsl[JPT / 2];
+#pragma unroll
+                        for (uint32_t h = 0; h < JPT / 2; ++h) {
+                            nsh[h] = psh[gi][h] ^ 0x80008000u;
+                            nsl[h] = psl[gi][h] ^ 0x80008000u;
+                        }
+                        unsigned char *zg = zh + gi * kRowNM;
+                        put(zg, nsh);
+                        put(zg + G::Z_BYTES, nsl);
+                        put(zg + ng * kRowNM, pch[gi]);
+                        put(zg + ng * kRowNM + G::Z_BYTES, pcl[gi]);
+                        put(zg + 2u * ng * kRowNM, psh[gi]);
+                        put(zg + 2u * ng * kRowNM + G::Z_BYTES, psl[gi]);
+                    }
                 }
-                // after the stage's last K-block: generic-proxy stores -> the MMA's
-                // async-proxy reads; then one arrival for the warp, after all its lanes
-                // have fenced
-                if (last) {
-                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    __syncwarp();
-                    if (lane == 0) mbar_arrive(&full_bar[s]);
-                    ++g;
-                }
+                // generic-proxy stores -> the MMA's async-proxy reads; then one arrival for
+                // the warp (also when the stage has no K-block for its group), after all its
+                // lanes have fenced
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&full_bar[s]);
+                ++g;
             }
+            if (!ok) break;
         }
     } else if (warp == kLoaderWarp) {
         // ---------------- operand loader ----------------
