@@ -89,7 +89,7 @@ struct TGeo {
     static constexpr int A_BYTES = kTP * kTK * 2;  // one 128 x 16 FP16 matrix
     static constexpr int Z_ROWS = 3 * G0 * NM;     // [-Bi; Br; Bi], each G rows blocks of NM
     static constexpr int Z_BYTES = Z_ROWS * kTK * 2;
-    // stage: KPS consecutive K-blocks of one phase, so that the MMA thread waits and
+    // stage: KPS consecutive K-blocks of one phase, so that the MMA warp waits and
     // commits once per 6 KPS MMAs: their A matrices (re/im, hi/lo; AKB bytes each), then
     // their Z matrices (hi, lo; ZKB bytes each)
     static constexpr int KPS = 2;
