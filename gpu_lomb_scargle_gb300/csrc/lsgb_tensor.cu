@@ -657,7 +657,8 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                         const uint32_t wre = gnm * (uint32_t)G::NM * 32u;
                         const uint32_t idesc = ph ? idesc1 : idesc0;
                         for (uint32_t kb = kb0; kb < kb1; kb += G::KPS) {  // one stage
-                            if (!__all_sync(0xffffffffu, mbar_wait(&full_bar[s], sph, &s_abort, a.status))) {
+                            if (!__all_sync(0xffffffffu,
+                                            mbar_wait(&full_bar[s], sph, &s_abort, a.status))) {
                                 ok = false;
                                 break;
                             }
