@@ -16,7 +16,8 @@ DROPIN_LIBS = ("libpylsnoerrorfloat.so", "libpylsnoerrordouble.so", "libpylserro
 # Symbols each library must export (the declarations of include/lsgb.h and
 # include/lombscargle_py.h).
 LSGB_SYMBOLS = ("lsgb_engine_create", "lsgb_engine_destroy", "lsgb_last_error", "lsgb_version",
-                "lsgb_periodogram_device", "lsgb_periodogram_host", "lsgb_set_tuning",
+                "lsgb_periodogram_device", "lsgb_periodogram_host", "lsgb_periodogram_top3_device",
+                "lsgb_periodogram_top3_host", "lsgb_set_tuning",
                 "lsgb_last_launch_info", "lsgb_last_kernel_time", "lsgb_mixed_shapes",
                 "lsgb_get_tuning", "lsgb_periodogram_noalloc", "lsgb_server_create",
                 "lsgb_server_submit", "lsgb_server_poll", "lsgb_server_stats", "lsgb_server_now",
@@ -64,6 +65,10 @@ def lsgb() -> ctypes.CDLL:
         lib.lsgb_periodogram_device.restype = i32
         lib.lsgb_periodogram_host.argtypes = common
         lib.lsgb_periodogram_host.restype = i32
+        lib.lsgb_periodogram_top3_device.argtypes = common + [vp]
+        lib.lsgb_periodogram_top3_device.restype = i32
+        lib.lsgb_periodogram_top3_host.argtypes = common
+        lib.lsgb_periodogram_top3_host.restype = i32
         lib.lsgb_set_tuning.argtypes = [vp, i32, i32, i32, i32, i32, i32]
         lib.lsgb_set_tuning.restype = i32
         lib.lsgb_last_launch_info.argtypes = [vp, c.POINTER(c.c_uint32), c.POINTER(c.c_uint64)]

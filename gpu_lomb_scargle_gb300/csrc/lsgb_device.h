@@ -47,6 +47,96 @@ __device__ __forceinline__ bool better(V p1, uint32_t k1, V p2, uint32_t k2) {
     return p1 > p2 || (p1 == p2 && k1 < k2);
 }
 
+// ---- the three best frequencies of an object (source/main.cu:1165-1219) ----
+// The reference scans the periodogram three times from (power 0, index 0), each scan
+// taking the first strictly larger power at an index the earlier scans did not take. So
+// its result is the three largest (power, lowest index) pairs among the positive powers,
+// in that order, padded with (0, index 0). With a positive FP32 power the key
+// (power bits << 32 | ~index) orders pairs that way as one unsigned integer (0: none).
+__device__ __forceinline__ unsigned long long rank_key(float p, uint32_t k) {
+    return ((unsigned long long)__float_as_uint(p) << 32) | (unsigned long long)(~k);
+}
+
+// A thread's or warp's three largest keys, t0 > t1 > t2 (0 = empty).
+struct Top3 {
+    unsigned long long t0 = 0ull, t1 = 0ull, t2 = 0ull;
+    // Offers a key (keys offered to one Top3 are distinct).
+    __device__ __forceinline__ void offer(unsigned long long x) {
+        if (x > t2) {
+            if (x > t1) {
+                t2 = t1;
+                if (x > t0) { t1 = t0; t0 = x; }
+                else t1 = x;
+            } else {
+                t2 = x;
+            }
+        }
+    }
+    // Offers a positive power at frequency index k.
+    __device__ __forceinline__ void offer(float p, uint32_t k) {
+        if (p > 0.0f) offer(rank_key(p, k));
+    }
+    // Merges the three keys of every lane of the (converged) warp into every lane. The
+    // butterfly pairs disjoint groups of lanes, so the keys merged are always distinct.
+    __device__ __forceinline__ void warp_merge() {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const unsigned long long u0 = __shfl_xor_sync(0xffffffffu, t0, off);
+            const unsigned long long u1 = __shfl_xor_sync(0xffffffffu, t1, off);
+            const unsigned long long u2 = __shfl_xor_sync(0xffffffffu, t2, off);
+            if (u0) offer(u0);
+            if (u1) offer(u1);
+            if (u2) offer(u2);
+        }
+    }
+};
+
+// Inserts key x into an object's global top three slots s[0] > s[1] > s[2] (zero-
+// initialized). Each level keeps the larger of what it holds and what arrives and passes
+// the smaller on: level 0 ends with the largest key ever inserted, level 1 with the
+// largest of the rest, and so on, whatever the interleaving of concurrent inserts. Keys
+// not above the current third slot are skipped with one plain load (slots only grow).
+__device__ __forceinline__ void top3_insert(unsigned long long *s, unsigned long long x) {
+    if (x == 0ull || x <= *(volatile unsigned long long *)(s + 2)) return;
+#pragma unroll
+    for (int i = 0; i < 3 && x != 0ull; ++i) {
+        const unsigned long long old = atomicMax(s + i, x);
+        x = old < x ? old : x;
+    }
+}
+
+// The same for (power, index) pairs of any type (the FP64 form keeps per-tile triples).
+template <typename V>
+struct Top3PK {
+    V p[3] = {V(0), V(0), V(0)};
+    uint32_t k[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu};  // 0xffffffff: empty
+    // Offers a pair; only positive powers count (the reference's scans start at 0).
+    __device__ __forceinline__ void offer(V q, uint32_t j) {
+        if (j == 0xffffffffu || !(q > V(0)) || !better(q, j, p[2], k[2])) return;
+        if (better(q, j, p[1], k[1])) {
+            p[2] = p[1]; k[2] = k[1];
+            if (better(q, j, p[0], k[0])) { p[1] = p[0]; k[1] = k[0]; p[0] = q; k[0] = j; }
+            else { p[1] = q; k[1] = j; }
+        } else {
+            p[2] = q; k[2] = j;
+        }
+    }
+    __device__ __forceinline__ void warp_merge() {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            V q[3];
+            uint32_t j[3];
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                q[r] = __shfl_xor_sync(0xffffffffu, p[r], off);
+                j[r] = __shfl_xor_sync(0xffffffffu, k[r], off);
+            }
+#pragma unroll
+            for (int r = 0; r < 3; ++r) offer(q[r], j[r]);
+        }
+    }
+};
+
 // Standard L-S power from the sums of one frequency (N observations):
 //   P = 1/2 [ (Q+U)/(N+r) + (Q-U)/(N-r) ],  Q = XC^2+XS^2,
 //   U = [ (CC-SS)(XC^2-XS^2) + 4 CS XC XS ] / r,  r = hypot(CC-SS, 2 CS),

@@ -107,6 +107,7 @@ struct Batch {
     MixedShape shape{};
     uint32_t reanchor = 0;
     bool want_best = false, fold = false;
+    uint32_t top = 1;  // best frequencies per object: 1 (argmax) or 3 (the top three)
     size_t smem = 0;
     int grid = 0;
     uint32_t kernels = 0;
@@ -118,7 +119,10 @@ struct Batch {
 int plan_batch(Batch &b, int sms, const MixedShape *shapes, uint32_t reanchor, int variant,
                int precision, int dtype, const void *t, const void *y, const void *dy,
                const uint64_t *offsets, uint32_t n_obj, double fmin, double df, uint32_t n_freq,
-               int normalize, void *pgram, uint32_t *best_idx, void *best_power) {
+               int normalize, void *pgram, uint32_t *best_idx, void *best_power,
+               uint32_t top = 1) {
+    if (top != 1 && top != 3) return fail(LSGB_ERR_INVALID, "top must be 1 or 3");
+    b.top = top;
     if (variant != LSGB_STANDARD && variant != LSGB_GENERALIZED)
         return fail(LSGB_ERR_INVALID, "variant %d is not LSGB_STANDARD or LSGB_GENERALIZED", variant);
     if (precision != LSGB_PLAIN_FP64 && precision != LSGB_MIXED)
@@ -239,8 +243,9 @@ int upload_tables(const Batch &b, Workspace &ws, cudaStream_t st) {
     LSGB_CUDA(ws.offs.ensure(sizeof(uint64_t) * (b.n_obj + 1)));
     LSGB_CUDA(ws.perm.ensure(sizeof(uint32_t) * b.n_obj));
     LSGB_CUDA(ws.counter.ensure(sizeof(uint32_t)));
-    if (b.want_best && !mixed) LSGB_CUDA(ws.tile_best.ensure(sizeof(TileBest) * b.units));
-    if (b.want_best && mixed) LSGB_CUDA(ws.keys.ensure(sizeof(unsigned long long) * b.n_obj));
+    if (b.want_best && !mixed) LSGB_CUDA(ws.tile_best.ensure(sizeof(TileBest) * b.units * b.top));
+    if (b.want_best && mixed)
+        LSGB_CUDA(ws.keys.ensure(sizeof(unsigned long long) * b.n_obj * b.top));
     if (mixed) LSGB_CUDA(ws.rec.ensure(mixed_global_rec_bytes(b.shape) * b.rows));
     if (mixed && b.shape.x2 == 3) LSGB_CUDA(ws.optab.ensure(tensor_optab_bytes(b.variant, b.total_kb)));
     if (mixed && !ws.status.p) {
@@ -284,7 +289,7 @@ int enqueue_batch(Batch &b, Workspace &ws, cudaStream_t st, cudaEvent_t ev0, cud
     uint32_t kernels = 0;
     LSGB_CUDA(cudaMemsetAsync(ws.counter.p, 0, sizeof(uint32_t), st));
     if (b.want_best && mixed)
-        LSGB_CUDA(cudaMemsetAsync(ws.keys.p, 0, sizeof(unsigned long long) * b.n_obj, st));
+        LSGB_CUDA(cudaMemsetAsync(ws.keys.p, 0, sizeof(unsigned long long) * b.n_obj * b.top, st));
     LSGB_CUDA(launch_stats(b.variant, mixed ? 1 : 0, b.dtype, b.normalize, b.y, b.dy, d_objs,
                            b.n_obj, st));
     ++kernels;
@@ -314,6 +319,7 @@ int enqueue_batch(Batch &b, Workspace &ws, cudaStream_t st, cudaEvent_t ev0, cud
         a.reanchor = b.reanchor;
         a.fold = b.fold ? 1u : 0u;
         a.status = (uint32_t *)ws.status.p;
+        a.top = b.top;
         if (b.shape.x2 == 3) {
             LSGB_CUDA(launch_tensor_optab(b.variant, a, b.total_kb, st));
             ++kernels;
@@ -338,18 +344,19 @@ int enqueue_batch(Batch &b, Workspace &ws, cudaStream_t st, cudaEvent_t ev0, cud
         a.counter = (uint32_t *)ws.counter.p;
         a.pgram = b.pgram;
         a.tile_best = b.want_best ? (TileBest *)ws.tile_best.p : nullptr;
+        a.top = b.top;
         if (ev0) LSGB_CUDA(record(ev0, st, capturing));
         LSGB_CUDA(launch_plain(b.variant, b.dtype, b.dtype, a, b.grid, b.smem, st));
         if (ev1) LSGB_CUDA(record(ev1, st, capturing));
         ++kernels;
     }
     if (b.want_best && mixed) {
-        LSGB_CUDA(launch_key_decode(b.dtype, (const unsigned long long *)ws.keys.p, b.n_obj,
-                                    b.best_idx, b.best_power, st));
+        LSGB_CUDA(launch_key_decode(b.dtype, (const unsigned long long *)ws.keys.p,
+                                    b.n_obj * b.top, b.best_idx, b.best_power, st));
         ++kernels;
     } else if (b.want_best) {
         LSGB_CUDA(launch_best_reduce(b.dtype, (const TileBest *)ws.tile_best.p, b.n_obj, b.n_tiles,
-                                     b.best_idx, b.best_power, st));
+                                     b.top, b.best_idx, b.best_power, st));
         ++kernels;
     }
     b.kernels = kernels;
@@ -506,11 +513,13 @@ LSGB_API int lsgb_last_kernel_time(lsgb_engine *eng, float *ms) {
     return check_status(eng->ws);
 }
 
-LSGB_API int lsgb_periodogram_device(lsgb_engine *eng, int variant, int precision, int dtype,
-                                     const void *t, const void *y, const void *dy,
-                                     const uint64_t *offsets, uint32_t n_obj, double fmin,
-                                     double df, uint32_t n_freq, int normalize, void *pgram,
-                                     uint32_t *best_idx, void *best_power, void *stream_) {
+// The device-buffer call with `top` (1 or 3) best frequencies per object: best_idx and
+// best_power hold [n_obj x top] entries, best first.
+static int periodogram_device(lsgb_engine *eng, int variant, int precision, int dtype,
+                              const void *t, const void *y, const void *dy,
+                              const uint64_t *offsets, uint32_t n_obj, double fmin, double df,
+                              uint32_t n_freq, int normalize, void *pgram, uint32_t *best_idx,
+                              void *best_power, void *stream_, uint32_t top) {
     if (!eng) return fail(LSGB_ERR_INVALID, "engine is NULL");
     eng->last_kernels = 0;
     eng->last_units = 0;
@@ -518,7 +527,8 @@ LSGB_API int lsgb_periodogram_device(lsgb_engine *eng, int variant, int precisio
     LSGB_CUDA(cudaSetDevice(eng->device));
     Batch b;
     int rc = plan_batch(b, eng->sms, eng->shape, eng->reanchor, variant, precision, dtype, t, y, dy,
-                        offsets, n_obj, fmin, df, n_freq, normalize, pgram, best_idx, best_power);
+                        offsets, n_obj, fmin, df, n_freq, normalize, pgram, best_idx, best_power,
+                        top);
     if (rc != LSGB_OK || b.empty) return rc;
     rc = upload_tables(b, eng->ws, st);
     if (rc != LSGB_OK) return rc;
@@ -528,6 +538,24 @@ LSGB_API int lsgb_periodogram_device(lsgb_engine *eng, int variant, int precisio
     eng->last_kernels = b.kernels;
     eng->last_units = b.units;
     return LSGB_OK;
+}
+
+LSGB_API int lsgb_periodogram_device(lsgb_engine *eng, int variant, int precision, int dtype,
+                                     const void *t, const void *y, const void *dy,
+                                     const uint64_t *offsets, uint32_t n_obj, double fmin,
+                                     double df, uint32_t n_freq, int normalize, void *pgram,
+                                     uint32_t *best_idx, void *best_power, void *stream) {
+    return periodogram_device(eng, variant, precision, dtype, t, y, dy, offsets, n_obj, fmin, df,
+                              n_freq, normalize, pgram, best_idx, best_power, stream, 1u);
+}
+
+LSGB_API int lsgb_periodogram_top3_device(lsgb_engine *eng, int variant, int precision, int dtype,
+                                          const void *t, const void *y, const void *dy,
+                                          const uint64_t *offsets, uint32_t n_obj, double fmin,
+                                          double df, uint32_t n_freq, int normalize, void *pgram,
+                                          uint32_t *top_idx, void *top_power, void *stream) {
+    return periodogram_device(eng, variant, precision, dtype, t, y, dy, offsets, n_obj, fmin, df,
+                              n_freq, normalize, pgram, top_idx, top_power, stream, 3u);
 }
 
 LSGB_API void lsgb_plan_destroy(lsgb_plan *p) {
@@ -609,12 +637,13 @@ LSGB_API int lsgb_plan_info(lsgb_plan *p, uint32_t *kernels, uint64_t *units, fl
     return LSGB_OK;
 }
 
-LSGB_API int lsgb_periodogram_host(lsgb_engine *eng, int variant, int precision, int dtype,
-                                   const void *t, const void *y, const void *dy,
-                                   const uint64_t *offsets, uint32_t n_obj, double fmin, double df,
-                                   uint32_t n_freq, int normalize, void *pgram, uint32_t *best_idx,
-                                   void *best_power) {
+// The host-buffer call with `top` (1 or 3) best frequencies per object.
+static int periodogram_host(lsgb_engine *eng, int variant, int precision, int dtype,
+                            const void *t, const void *y, const void *dy, const uint64_t *offsets,
+                            uint32_t n_obj, double fmin, double df, uint32_t n_freq, int normalize,
+                            void *pgram, uint32_t *best_idx, void *best_power, uint32_t top) {
     if (!eng) return fail(LSGB_ERR_INVALID, "engine is NULL");
+    if (top != 1 && top != 3) return fail(LSGB_ERR_INVALID, "top must be 1 or 3");
     if (!offsets || n_obj == 0) return fail(LSGB_ERR_INVALID, "offsets is NULL or n_obj is 0");
     if (dtype != LSGB_F32 && dtype != LSGB_F64)
         return fail(LSGB_ERR_INVALID, "dtype %d is not LSGB_F32 or LSGB_F64", dtype);
@@ -643,11 +672,11 @@ LSGB_API int lsgb_periodogram_host(lsgb_engine *eng, int variant, int precision,
         d_pg = eng->out_pg.p;
     }
     if (best_idx) {
-        LSGB_CUDA(eng->out_idx.ensure(sizeof(uint32_t) * n_obj));
+        LSGB_CUDA(eng->out_idx.ensure(sizeof(uint32_t) * n_obj * top));
         d_idx = (uint32_t *)eng->out_idx.p;
     }
     if (best_power) {
-        LSGB_CUDA(eng->out_p.ensure(es * n_obj));
+        LSGB_CUDA(eng->out_p.ensure(es * n_obj * top));
         d_p = eng->out_p.p;
     }
     // A large periodogram goes out in object chunks: every chunk's computation is queued
@@ -676,14 +705,14 @@ LSGB_API int lsgb_periodogram_host(lsgb_engine *eng, int variant, int precision,
             LSGB_CUDA(eng->ws.offs.ensure(sizeof(uint64_t) * (n_obj + 1)));
             LSGB_CUDA(eng->ws.perm.ensure(sizeof(uint32_t) * n_obj));
             LSGB_CUDA(eng->ws.counter.ensure(sizeof(uint32_t)));
-            LSGB_CUDA(eng->ws.keys.ensure(sizeof(unsigned long long) * n_obj));
+            LSGB_CUDA(eng->ws.keys.ensure(sizeof(unsigned long long) * n_obj * top));
             if (precision == LSGB_MIXED)
                 LSGB_CUDA(eng->ws.rec.ensure(mixed_global_rec_bytes(eng->shape[variant]) * rows));
             if (precision == LSGB_MIXED && eng->shape[variant].x2 == 3)
                 LSGB_CUDA(eng->ws.optab.ensure(
                     tensor_optab_bytes(variant, rows / kTensorKBlock + n_obj)));
             else if (best_idx || best_power)
-                LSGB_CUDA(eng->ws.tile_best.ensure(sizeof(TileBest) * max_tiles * n_obj));
+                LSGB_CUDA(eng->ws.tile_best.ensure(sizeof(TileBest) * max_tiles * n_obj * top));
         }
         std::vector<cudaEvent_t> ev(cut.size() - 1, nullptr);
         int rc = LSGB_OK;
@@ -692,12 +721,12 @@ LSGB_API int lsgb_periodogram_host(lsgb_engine *eng, int variant, int precision,
             const uint64_t r0 = offsets[o0];
             std::vector<uint64_t> offs_c(offsets + o0, offsets + o1 + 1);
             for (auto &v : offs_c) v -= r0;
-            rc = lsgb_periodogram_device(
+            rc = periodogram_device(
                 eng, variant, precision, dtype, (const char *)eng->in_t.p + es * r0,
                 (const char *)eng->in_y.p + es * r0, d_dy ? (const char *)d_dy + es * r0 : nullptr,
                 offs_c.data(), o1 - o0, fmin, df, n_freq, normalize,
-                (char *)d_pg + es * (uint64_t)o0 * n_freq, d_idx ? d_idx + o0 : nullptr,
-                d_p ? (char *)d_p + es * o0 : nullptr, (void *)st);
+                (char *)d_pg + es * (uint64_t)o0 * n_freq, d_idx ? d_idx + (uint64_t)o0 * top : nullptr,
+                d_p ? (char *)d_p + es * o0 * top : nullptr, (void *)st, top);
             if (rc == LSGB_OK) {
                 cudaError_t e = cudaEventCreateWithFlags(&ev[c], cudaEventDisableTiming);
                 if (e == cudaSuccess) e = cudaEventRecord(ev[c], st);
@@ -719,31 +748,52 @@ LSGB_API int lsgb_periodogram_host(lsgb_engine *eng, int variant, int precision,
             if (x) cudaEventDestroy(x);
         if (rc != LSGB_OK) return rc;
         if (d_idx)
-            LSGB_CUDA(cudaMemcpyAsync(best_idx, d_idx, sizeof(uint32_t) * n_obj, cudaMemcpyDeviceToHost, st));
-        if (d_p) LSGB_CUDA(cudaMemcpyAsync(best_power, d_p, es * n_obj, cudaMemcpyDeviceToHost, st));
+            LSGB_CUDA(cudaMemcpyAsync(best_idx, d_idx, sizeof(uint32_t) * n_obj * top,
+                                      cudaMemcpyDeviceToHost, st));
+        if (d_p)
+            LSGB_CUDA(cudaMemcpyAsync(best_power, d_p, es * n_obj * top, cudaMemcpyDeviceToHost, st));
         LSGB_CUDA(cudaStreamSynchronize(st));
         return check_status(eng->ws);
     }
-    int rc = lsgb_periodogram_device(eng, variant, precision, dtype, eng->in_t.p, eng->in_y.p, d_dy,
-                                     offsets, n_obj, fmin, df, n_freq, normalize, d_pg, d_idx, d_p,
-                                     (void *)st);
+    int rc = periodogram_device(eng, variant, precision, dtype, eng->in_t.p, eng->in_y.p, d_dy,
+                                offsets, n_obj, fmin, df, n_freq, normalize, d_pg, d_idx, d_p,
+                                (void *)st, top);
     if (rc != LSGB_OK) {
         cudaStreamSynchronize(st);
         return rc;
     }
     if (n_freq == 0) {
         // nothing computed: report index 0 / power 0 as the reference's argmax would
-        if (best_idx) memset(best_idx, 0, sizeof(uint32_t) * n_obj);
-        if (best_power) memset(best_power, 0, es * n_obj);
+        if (best_idx) memset(best_idx, 0, sizeof(uint32_t) * n_obj * top);
+        if (best_power) memset(best_power, 0, es * n_obj * top);
         LSGB_CUDA(cudaStreamSynchronize(st));
         return LSGB_OK;
     }
     if (d_pg) LSGB_CUDA(cudaMemcpyAsync(pgram, d_pg, es * pg_elems, cudaMemcpyDeviceToHost, st));
     if (d_idx)
-        LSGB_CUDA(cudaMemcpyAsync(best_idx, d_idx, sizeof(uint32_t) * n_obj, cudaMemcpyDeviceToHost, st));
-    if (d_p) LSGB_CUDA(cudaMemcpyAsync(best_power, d_p, es * n_obj, cudaMemcpyDeviceToHost, st));
+        LSGB_CUDA(cudaMemcpyAsync(best_idx, d_idx, sizeof(uint32_t) * n_obj * top,
+                                  cudaMemcpyDeviceToHost, st));
+    if (d_p) LSGB_CUDA(cudaMemcpyAsync(best_power, d_p, es * n_obj * top, cudaMemcpyDeviceToHost, st));
     LSGB_CUDA(cudaStreamSynchronize(st));
     return check_status(eng->ws);
+}
+
+LSGB_API int lsgb_periodogram_host(lsgb_engine *eng, int variant, int precision, int dtype,
+                                   const void *t, const void *y, const void *dy,
+                                   const uint64_t *offsets, uint32_t n_obj, double fmin, double df,
+                                   uint32_t n_freq, int normalize, void *pgram, uint32_t *best_idx,
+                                   void *best_power) {
+    return periodogram_host(eng, variant, precision, dtype, t, y, dy, offsets, n_obj, fmin, df,
+                            n_freq, normalize, pgram, best_idx, best_power, 1u);
+}
+
+LSGB_API int lsgb_periodogram_top3_host(lsgb_engine *eng, int variant, int precision, int dtype,
+                                        const void *t, const void *y, const void *dy,
+                                        const uint64_t *offsets, uint32_t n_obj, double fmin,
+                                        double df, uint32_t n_freq, int normalize, void *pgram,
+                                        uint32_t *top_idx, void *top_power) {
+    return periodogram_host(eng, variant, precision, dtype, t, y, dy, offsets, n_obj, fmin, df,
+                            n_freq, normalize, pgram, top_idx, top_power, 3u);
 }
 
 }  // extern "C"

@@ -89,8 +89,9 @@ struct MixedArgs {
     TileBest *tile_best;   // [n_obj x n_tiles] or null
     uint32_t reanchor;     // 0: anchor at every thread's run start; R > 0: anchor every R
                            // grid points and reach the run start by the FP32 recurrence
-    unsigned long long *best_key;  // [n_obj] packed (power bits << 32 | ~index) maxima, or
-                                   // null to use tile_best; zero means "no positive power"
+    unsigned long long *best_key;  // [n_obj x top] packed (power bits << 32 | ~index) maxima
+                                   // (the `top` best of each object, best first), or null
+                                   // to use tile_best; zero means "no positive power"
     uint32_t fold;         // 1: shared memory holds a second-level sum area after the records
                            // (objects longer than `chunk` fold their chunk sums into it)
     uint32_t *status;      // tensor form: bit 0 set when a bounded pipeline wait timed out
@@ -99,6 +100,7 @@ struct MixedArgs {
     const void *steps;     // the K-blocks' steps arrays (tensor_step_bytes each); both
                            // filled by launch_tensor_optab for this batch
     uint32_t total_kb;     // tensor form: K-blocks of the batch (the table's phase stride)
+    uint32_t top;          // best frequencies kept per object: 1 (argmax) or 3
 };
 
 
@@ -110,7 +112,8 @@ struct PlainArgs {
     double fmin, df;
     uint32_t *counter;
     void *pgram;
-    TileBest *tile_best;
+    TileBest *tile_best;   // [n_obj x n_tiles x top]: each tile's `top` best, best first
+    uint32_t top;          // 1 or 3
 };
 
 // Compiled tile shapes of the mixed kernel: frequencies per thread, threads per CTA,
@@ -171,14 +174,17 @@ int mixed_shapes(int *out, int max_shapes);
 cudaError_t launch_plain(int variant, int in_dtype, int out_dtype, const PlainArgs &a, int grid,
                          size_t smem, cudaStream_t st);
 cudaError_t plain_occupancy(int variant, int in_dtype, int out_dtype, size_t smem, int *blocks);
+// Per-object best `top` (1 or 3) frequencies from the tiles' results: best_idx and
+// best_power are [n_obj x top], best first.
 cudaError_t launch_best_reduce(int dtype, const TileBest *tb, uint32_t n_obj, uint32_t n_tiles,
-                               uint32_t *best_idx, void *best_power, cudaStream_t st);
+                               uint32_t top, uint32_t *best_idx, void *best_power, cudaStream_t st);
 // Largest |difference| of the plain kernel's FP64 sine/cosine from sincos() over n
 // arguments spread over [-scale, scale]; *max_err (device) must start at 0.
 cudaError_t launch_sincos_check(uint32_t n, uint64_t seed, double scale, double *max_err,
                                 cudaStream_t st);
-// Unpacks MixedArgs::best_key maxima into (index, power).
-cudaError_t launch_key_decode(int dtype, const unsigned long long *keys, uint32_t n_obj,
+// Unpacks n packed keys (MixedArgs::best_key) into (index, power); an empty key gives
+// (0, 0).
+cudaError_t launch_key_decode(int dtype, const unsigned long long *keys, uint32_t n,
                               uint32_t *best_idx, void *best_power, cudaStream_t st);
 
 constexpr int kPlainThreads = 256;

@@ -578,6 +578,8 @@ __global__ void __launch_bounds__(NT, MINB) mixed_kernel(MixedArgs a) {
         float bp = 0.0f;
         uint32_t bk = 0xffffffffu;
         if (tile == 0 && threadIdx.x == 0) bk = 0;  // the reference's (power 0, index 0) start
+        const bool top3 = a.top == 3u;  // keep the three best instead of the maximum
+        Top3 t3;
         const uint64_t out0 = (uint64_t)o * a.n_freq;
         const float nrm = a.objs[o].norm32;
         if (!GEN) {
@@ -588,7 +590,8 @@ __global__ void __launch_bounds__(NT, MINB) mixed_kernel(MixedArgs a) {
                 const float P = std_power_f(N, acc[0][f], acc[1][f], acc[2][f], acc[3][f]) * nrm;
                 if (k < a.n_freq) {
                     if (a.pgram) store_out<OutT>(a.pgram, out0 + k, P);
-                    if (P > bp) { bp = P; bk = k; }
+                    if (top3) t3.offer(P, k);
+                    else if (P > bp) { bp = P; bk = k; }
                 }
             }
         } else {
@@ -601,11 +604,21 @@ __global__ void __launch_bounds__(NT, MINB) mixed_kernel(MixedArgs a) {
                                             acc[4][f], acc[5][f]) * nrm;
                 if (k < a.n_freq) {
                     if (a.pgram) store_out<OutT>(a.pgram, out0 + k, P);
-                    if (P > bp) { bp = P; bk = k; }
+                    if (top3) t3.offer(P, k);
+                    else if (P > bp) { bp = P; bk = k; }
                 }
             }
         }
-        if (a.best_key) {
+        if (a.best_key && top3) {
+            // the warp's three best, then into the object's three slots
+            t3.warp_merge();
+            if ((threadIdx.x & 31) == 0) {
+                unsigned long long *slots = a.best_key + 3ull * o;
+                top3_insert(slots, t3.t0);
+                top3_insert(slots, t3.t1);
+                top3_insert(slots, t3.t2);
+            }
+        } else if (a.best_key) {
             // warp maximum, then one 64-bit atomicMax per warp: larger power wins, and on
             // equal power the larger ~index, i.e. the lower index (the first maximum)
 #pragma unroll
@@ -716,6 +729,8 @@ __global__ void __launch_bounds__(NT) plain_kernel(PlainArgs a) {
     __shared__ uint32_t s_unit;
     __shared__ double s_bp[NT / 32];
     __shared__ uint32_t s_bk[NT / 32];
+    __shared__ double s_bp3[3 * (NT / 32)];     // top-3 per warp (PlainArgs::top == 3)
+    __shared__ uint32_t s_bk3[3 * (NT / 32)];
     __shared__ double2 s_tab[128];
     fill_sincos_table(s_tab);  // made visible by the first barrier of the unit loop
     const InT *T = reinterpret_cast<const InT *>(a.t);
@@ -850,12 +865,42 @@ __global__ void __launch_bounds__(NT) plain_kernel(PlainArgs a) {
         double bp = 0.0;
         uint32_t bk = 0xffffffffu;
         if (tile == 0 && threadIdx.x == 0) bk = 0;
+        double Pr = 0.0;
         if (k < a.n_freq) {
             if (a.pgram) store_out_d<OutT>(a.pgram, (uint64_t)o * a.n_freq + k, P);
-            const double Pr = (double)(OutT)P;  // compare in the output precision
+            Pr = (double)(OutT)P;  // compare in the output precision
             if (Pr > bp) { bp = Pr; bk = k; }
         }
-        if (a.tile_best) {
+        if (a.tile_best && a.top == 3u) {
+            // the tile's three best: per warp, then warp 0 over the warps' triples (constant
+            // indices throughout, so that the triples stay in registers)
+            Top3PK<double> t3;
+            if (k < a.n_freq) t3.offer(Pr, k);
+            t3.warp_merge();
+            const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+            if (l == 0) {
+#pragma unroll
+                for (int r = 0; r < 3; ++r) { s_bp3[w * 3 + r] = t3.p[r]; s_bk3[w * 3 + r] = t3.k[r]; }
+            }
+            __syncthreads();
+            if (w == 0) {
+                Top3PK<double> m;
+                if (l < NT / 32)
+#pragma unroll
+                    for (int r = 0; r < 3; ++r) m.offer(s_bp3[l * 3 + r], s_bk3[l * 3 + r]);
+                m.warp_merge();
+                if (l == 0) {
+#pragma unroll
+                    for (int r = 0; r < 3; ++r) {
+                        TileBest tb;
+                        tb.p = m.p[r];
+                        tb.k = m.k[r];
+                        tb.pad = 0;
+                        a.tile_best[((uint64_t)o * a.n_tiles + tile) * 3u + (uint32_t)r] = tb;
+                    }
+                }
+            }
+        } else if (a.tile_best) {
             block_best<NT, double>(bp, bk, s_bp, s_bk);
             if (threadIdx.x == 0) {
                 TileBest tb;
@@ -894,6 +939,30 @@ __global__ void best_reduce_kernel(const TileBest *tb, uint32_t n_obj, uint32_t 
     if (lane == 0) {
         if (best_idx) best_idx[warp] = bk == 0xffffffffu ? 0u : bk;
         if (best_power) best_power[warp] = (OutT)bp;
+    }
+}
+
+// The same for the tiles' top-3 triples: the object's three best (power, lowest index)
+// pairs, best first, (0, 0) where fewer than three positive powers exist.
+template <typename OutT>
+__global__ void best3_reduce_kernel(const TileBest *tb, uint32_t n_obj, uint32_t n_tiles,
+                                    uint32_t *best_idx, OutT *best_power) {
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= n_obj) return;
+    Top3PK<double> t3;
+    for (uint32_t i = lane; i < n_tiles * 3u; i += 32) {
+        const TileBest x = tb[(uint64_t)warp * n_tiles * 3u + i];
+        t3.offer(x.p, x.k);
+    }
+    t3.warp_merge();
+    if (lane == 0) {
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            const bool none = t3.k[r] == 0xffffffffu;
+            if (best_idx) best_idx[3ull * warp + r] = none ? 0u : t3.k[r];
+            if (best_power) best_power[3ull * warp + r] = none ? OutT(0) : (OutT)t3.p[r];
+        }
     }
 }
 
@@ -1098,10 +1167,20 @@ cudaError_t launch_key_decode(int dtype, const unsigned long long *keys, uint32_
 }
 
 cudaError_t launch_best_reduce(int dtype, const TileBest *tb, uint32_t n_obj, uint32_t n_tiles,
-                               uint32_t *best_idx, void *best_power, cudaStream_t st) {
+                               uint32_t top, uint32_t *best_idx, void *best_power, cudaStream_t st) {
     if (n_obj == 0) return cudaSuccess;
     const int threads = 256;
     const int blocks = (int)((n_obj * 32ull + threads - 1) / threads);
+    if (top == 3u) {
+        if (dtype == 0)
+            best3_reduce_kernel<float><<<blocks, threads, 0, st>>>(tb, n_obj, n_tiles, best_idx,
+                                                                   (float *)best_power);
+        else
+            best3_reduce_kernel<double><<<blocks, threads, 0, st>>>(tb, n_obj, n_tiles, best_idx,
+                                                                    (double *)best_power);
+        return cudaGetLastError();
+    }
+    if (top != 1u) return cudaErrorInvalidValue;
     if (dtype == 0)
         best_reduce_kernel<float><<<blocks, threads, 0, st>>>(tb, n_obj, n_tiles, best_idx,
                                                               (float *)best_power);

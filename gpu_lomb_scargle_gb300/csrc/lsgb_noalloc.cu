@@ -183,8 +183,26 @@ extern "C" LSGB_API int lsgb_periodogram_noalloc(int variant, int dtype, const v
     if ((e = launch_records(variant, dtype, t, y, dy, d_offs, n_obj, d_objs, rows, g, d_rec, 0u, st)) !=
         cudaSuccess)
         return fail_cuda("records kernel", e);
-    const uint32_t chunk = std::min<uint32_t>(max_n, kMixedSmemMax / (uint32_t)mixed_rec_bytes(shape));
-    const size_t smem = (size_t)mixed_rec_bytes(shape) * chunk;
+    // Shared memory as the engine sizes it: staged observations up to what keeps the
+    // shape's CTAs per SM resident, and for objects longer than one chunk a second-level
+    // sum area after them (the chunk sums are folded there, so no long FP32 sum forms).
+    int smem_sm = 0;
+    if ((e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) !=
+        cudaSuccess)
+        return fail_cuda("cudaDeviceGetAttribute", e);
+    const size_t per_cta = (size_t)smem_sm / (size_t)std::max(1, shape.minb) - 1024 - 256;
+    const uint32_t rec_bytes = (uint32_t)mixed_rec_bytes(shape);
+    size_t rec_budget = std::min<size_t>(kMixedSmemMax, per_cta);
+    uint32_t chunk = (uint32_t)std::min<size_t>(max_n, rec_budget / rec_bytes);
+    const bool fold = max_n > chunk;
+    const size_t fold_bytes = fold ? mixed_fold_bytes(variant, shape) : 0;
+    if (fold) {
+        rec_budget = per_cta >= fold_bytes + 64 * (size_t)rec_bytes
+                         ? std::min<size_t>(kMixedSmemMax, per_cta - fold_bytes)
+                         : 64 * (size_t)rec_bytes;
+        chunk = (uint32_t)std::min<size_t>(max_n, rec_budget / rec_bytes);
+    }
+    const size_t smem = (size_t)rec_bytes * chunk + fold_bytes;
     int occ = 0, sms = 0;
     if ((e = mixed_occupancy(variant, dtype, shape, smem, &occ)) != cudaSuccess)
         return fail_cuda("occupancy query", e);
@@ -199,14 +217,16 @@ extern "C" LSGB_API int lsgb_periodogram_noalloc(int variant, int dtype, const v
     a.n_tiles = (uint32_t)n_tiles;
     a.n_freq = n_freq;
     a.chunk = chunk;
+    a.fold = fold ? 1u : 0u;
     a.counter = d_counter;
     a.pgram = pgram;
     a.tile_best = want_best ? d_tb : nullptr;
+    a.top = 1u;
     const int grid = (int)std::min<uint64_t>((uint64_t)sms * (occ > 0 ? occ : 1), units);
     if ((e = launch_mixed(variant, dtype, shape, a, grid, smem, st)) != cudaSuccess)
         return fail_cuda("periodogram kernel", e);
     if (want_best &&
-        (e = launch_best_reduce(dtype, d_tb, n_obj, (uint32_t)n_tiles, best_idx, best_power, st)) !=
+        (e = launch_best_reduce(dtype, d_tb, n_obj, (uint32_t)n_tiles, 1u, best_idx, best_power, st)) !=
             cudaSuccess)
         return fail_cuda("argmax kernel", e);
     return LSGB_OK;

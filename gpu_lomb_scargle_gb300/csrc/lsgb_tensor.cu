@@ -803,6 +803,8 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             float bp = 0.0f;
             uint32_t bk = 0xffffffffu;
             if (w.tile == 0 && pl == 0 && eh == 0) bk = 0;  // the reference's (power 0, index 0) start
+            const bool top3 = a.top == 3u;  // keep the three best instead of the maximum
+            Top3 t3;
             // quantities: phase 0 groups (re, im) then phase 1 (re, im)
             constexpr int NQ = GEN ? 6 : 4;
             // frequencies per chunk: 16 for the standard variant (eight independent packed
@@ -864,16 +866,22 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
 #pragma unroll
                         for (int i = 0; i < CHK; ++i) store_out<OutT>(a.pgram, out0 + k0 + (uint32_t)kTP * (uint32_t)i, P[i]);
                     }
+                    if (top3) {
 #pragma unroll
-                    for (int i = 0; i < CHK; ++i)
-                        if (P[i] > bp) { bp = P[i]; bk = k0 + (uint32_t)kTP * (uint32_t)i; }
+                        for (int i = 0; i < CHK; ++i) t3.offer(P[i], k0 + (uint32_t)kTP * (uint32_t)i);
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < CHK; ++i)
+                            if (P[i] > bp) { bp = P[i]; bk = k0 + (uint32_t)kTP * (uint32_t)i; }
+                    }
                 } else {
 #pragma unroll
                     for (int i = 0; i < CHK; ++i) {
                         const uint32_t k = k0 + (uint32_t)kTP * (uint32_t)i;
                         if (k < a.n_freq) {
                             if (a.pgram) store_out<OutT>(a.pgram, out0 + k, P[i]);
-                            if (P[i] > bp) { bp = P[i]; bk = k; }
+                            if (top3) t3.offer(P[i], k);
+                            else if (P[i] > bp) { bp = P[i]; bk = k; }
                         }
                     }
                 }
@@ -887,7 +895,16 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             }
             ring.push(rsum[0]);
             ring.push(rsum[1]);
-            if (a.best_key) {
+            if (a.best_key && top3) {
+                // the warp's three best, then into the object's three slots
+                t3.warp_merge();
+                if (lane == 0) {
+                    unsigned long long *slots = a.best_key + 3ull * w.o;
+                    top3_insert(slots, t3.t0);
+                    top3_insert(slots, t3.t1);
+                    top3_insert(slots, t3.t2);
+                }
+            } else if (a.best_key) {
 #pragma unroll
                 for (int off = 16; off > 0; off >>= 1) {
                     const float op = __shfl_xor_sync(0xffffffffu, bp, off);

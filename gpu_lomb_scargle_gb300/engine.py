@@ -141,6 +141,23 @@ class Engine:
         return Plan(self, variant, precision, t, y, dy, offsets, fmin, df, n_freq, normalize,
                     pgram, best_idx, best_power)
 
+    def run_device_top3(self, variant, precision, t, y, dy, offsets, fmin, df, n_freq,
+                        normalize=True, pgram=None, top_idx=None, top_power=None, stream=None):
+        """As run_device, with the three best frequencies per object: top_idx (int32/uint32)
+        and top_power are CUDA tensors of n_obj x 3 (source/main.cu:1165-1219)."""
+        import torch
+
+        code = F32 if t.dtype == torch.float32 else F64
+        offs = np.ascontiguousarray(offsets, dtype=np.uint64)
+        ptr = lambda x: ctypes.c_void_p(x.data_ptr()) if x is not None else None
+        st = ctypes.c_void_p(stream.cuda_stream if stream is not None
+                             else torch.cuda.current_stream().cuda_stream)
+        self._check(self._lib.lsgb_periodogram_top3_device(
+            self._h, int(variant), _precision(precision), code, ptr(t), ptr(y), ptr(dy),
+            offs.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), offs.size - 1, float(fmin),
+            float(df), int(n_freq), int(bool(normalize)), ptr(pgram), ptr(top_idx), ptr(top_power),
+            st))
+
     # ---- host-buffer call -----------------------------------------------------
     def run_host(self, variant, precision, t, y, dy, offsets, fmin, df, n_freq, normalize=True,
                  want_pgram=False, out_pgram=None, out_idx=None, out_power=None) -> Result:
@@ -161,6 +178,26 @@ class Engine:
             offs.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), n_obj, float(fmin), float(df),
             int(n_freq), int(bool(normalize)), vp(pg), vp(idx), vp(pw))
         self._check(rc)
+        return Result(idx, pw, pg)
+
+    def run_host_top3(self, variant, precision, t, y, dy, offsets, fmin, df, n_freq,
+                      normalize=True, want_pgram=False) -> Result:
+        """As run_host, with best_idx / best_power of shape (n_obj, 3): the three best
+        frequencies of every object, best first (0 where fewer than three positive powers)."""
+        t = np.ascontiguousarray(t)
+        code = _dtype_code(t.dtype)
+        y = np.ascontiguousarray(y, dtype=t.dtype)
+        dy = None if dy is None else np.ascontiguousarray(dy, dtype=t.dtype)
+        offs = np.ascontiguousarray(offsets, dtype=np.uint64)
+        n_obj = offs.size - 1
+        pg = np.empty((n_obj, int(n_freq)), dtype=t.dtype) if want_pgram else None
+        idx = np.empty((n_obj, 3), np.uint32)
+        pw = np.empty((n_obj, 3), t.dtype)
+        vp = lambda a: a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+        self._check(self._lib.lsgb_periodogram_top3_host(
+            self._h, int(variant), _precision(precision), code, vp(t), vp(y), vp(dy),
+            offs.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), n_obj, float(fmin), float(df),
+            int(n_freq), int(bool(normalize)), vp(pg), vp(idx), vp(pw)))
         return Result(idx, pw, pg)
 
 

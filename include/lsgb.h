@@ -89,6 +89,29 @@ LSGB_API int lsgb_periodogram_host(lsgb_engine *eng, int variant, int precision,
                                    uint32_t n_freq, int normalize, void *pgram, uint32_t *best_idx,
                                    void *best_power);
 
+/* The three best frequencies of every object, found on the device in the same kernel
+ * pass (no periodogram copy needed). Replaces the reference's PRINTPERIODS==3 host scans
+ * over the returned periodogram (source/main.cu:1165-1219, written out by
+ * outputPeriodsToFileTopThree :982-995): three scans from (power 0, index 0), each taking
+ * the first strictly larger power at an index the earlier scans did not take. So:
+ *   top_idx    [n_obj x 3] uint32 (or NULL): per object the indices of its three largest
+ *              positive powers, best first, the lowest index first among equal powers;
+ *              0 where the object has fewer than three positive powers.
+ *   top_power  [n_obj x 3] (dtype, or NULL): those powers (0 where there is none).
+ * Other arguments as lsgb_periodogram_device / lsgb_periodogram_host; top_idx[3*o] and
+ * top_power[3*o] are exactly what they return as best_idx[o] and best_power[o]. */
+LSGB_API int lsgb_periodogram_top3_device(lsgb_engine *eng, int variant, int precision, int dtype,
+                                          const void *t, const void *y, const void *dy,
+                                          const uint64_t *offsets_host, uint32_t n_obj,
+                                          double fmin, double df, uint32_t n_freq, int normalize,
+                                          void *pgram, uint32_t *top_idx, void *top_power,
+                                          void *stream);
+LSGB_API int lsgb_periodogram_top3_host(lsgb_engine *eng, int variant, int precision, int dtype,
+                                        const void *t, const void *y, const void *dy,
+                                        const uint64_t *offsets, uint32_t n_obj, double fmin,
+                                        double df, uint32_t n_freq, int normalize, void *pgram,
+                                        uint32_t *top_idx, void *top_power);
+
 /* ---- execution plans: one batch shape, captured once in a CUDA graph ----
  * lsgb_plan_create plans a batch exactly as lsgb_periodogram_device would (same
  * arguments; device pointers are fixed into the plan), uploads its per-object tables

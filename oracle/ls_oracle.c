@@ -175,6 +175,26 @@ LSO_API void lso_argmax(const double *p, uint32_t nf, uint32_t *idx, double *pow
     *power = maxp;
 }
 
+/* The three best frequencies, source/main.cu:1165-1219 (PRINTPERIODS==3): three
+ * scans from (power 0, index 0), each with the strict '<' of the argmax, the second
+ * skipping the first's index and the third skipping both earlier indices. */
+LSO_API void lso_top3(const double *p, uint32_t nf, uint32_t *idx, double *power) {
+    double maxp[3] = {0.0, 0.0, 0.0};
+    uint32_t maxi[3] = {0, 0, 0};
+    for (int r = 0; r < 3; r++) {
+        for (uint32_t j = 0; j < nf; j++) {
+            if (r >= 1 && j == maxi[0]) continue;
+            if (r >= 2 && j == maxi[1]) continue;
+            if (maxp[r] < p[j]) {
+                maxp[r] = p[j];
+                maxi[r] = j;
+            }
+        }
+        idx[r] = maxi[r];
+        power[r] = maxp[r];
+    }
+}
+
 /* Batch periodogram on a subset of grid indices.
  *   variant 0: standard (source/main.cu:1469-1502, normalized when normalize!=0
  *              as the Python builds do, :1497-1499);

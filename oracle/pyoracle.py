@@ -49,6 +49,7 @@ def _load():
     lib.lso_omega.restype = ctypes.c_double
     lib.lso_argmax.argtypes = [dp, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32),
                                ctypes.POINTER(ctypes.c_double)]
+    lib.lso_top3.argtypes = [dp, ctypes.c_uint32, up, dp]
     lib.lso_max_threads.restype = ctypes.c_int
     _lib = lib
     return lib
@@ -107,6 +108,17 @@ def argmax(p):
     v = ctypes.c_double()
     lib.lso_argmax(p, p.size, ctypes.byref(i), ctypes.byref(v))
     return int(i.value), float(v.value)
+
+
+def top3(p):
+    """The three best (index, power) pairs, best first, by the reference's three scans
+    (source/main.cu:1165-1219): arrays (idx[3], power[3])."""
+    lib = _load()
+    p = np.ascontiguousarray(p, dtype=np.float64)
+    idx = np.zeros(3, np.uint32)
+    pw = np.zeros(3, np.float64)
+    lib.lso_top3(p, p.size, idx, pw)
+    return idx, pw
 
 
 def float_grid(min_freq: float, max_freq: float, n_freq: int):
