@@ -112,8 +112,9 @@ def build(force: bool = False, jobs: int = 0, verbose: bool = False) -> Path:
         link_steps.append((link + [str(o), str(k_obj), str(t_obj), str(e_obj), "-o", str(LIB / lib)],
                            LIB / lib, [o, k_obj, t_obj, e_obj]))
     cli = LIB / "lsgb_main"
-    link_steps.append(([nv, *NVCC_COMMON, "-O2", str(CSRC / "lsgb_cli.cpp"), "-o", str(cli), "-ldl"],
-                       cli, [CSRC / "lsgb_cli.cpp"]))
+    link_steps.append(([nv, *NVCC_COMMON, *HOST_FLAGS, "-O2", str(CSRC / "lsgb_cli.cpp"), "-o",
+                        str(cli), "-ldl"],
+                       cli, [CSRC / "lsgb_cli.cpp", CSRC / "lsgb_cpu.h", INCLUDE / "lsgb.h"]))
     with cf.ThreadPoolExecutor(jobs) as ex:
         for f in [ex.submit(_run, c, force, o, d) for c, o, d in link_steps]:
             f.result()

@@ -1,5 +1,4 @@
-// lsgb_cli.cpp -- lsgb_main, the reference's command-line front ends over the drop-in
-// libraries.
+// lsgb_cli.cpp -- lsgb_main, the reference's command-line front ends over this engine.
 //
 // Two syntaxes, as the reference's two programs have:
 //   paper   (source/main.cu:92-252):
@@ -13,16 +12,26 @@
 //                      has 4 columns
 //   -d, --double       double build (default: double for the paper syntax, float for the
 //                      release syntax, as the reference programs default)
+//   -nrp, --normpgram  normalize the standard periodogram by 2/(N var(y)); by default it is
+//                      left unnormalized, as the reference's programs do (source/params.h:40
+//                      NORMALIZEPGRAM 0, release/main.cu:376)
+//   -n, --nthreads <k> CPU threads of the CPU modes (release/main.cu:330)
+//   -ng, --ngpus <k>   accepted for the release syntax; this engine runs on one GPU
 //   -ps, --printscreen             periods to stdout
 //   -pf, --printfile <file>        periods to <file> (the paper's bestperiods.txt layout)
-//   --top3 <file>                  top three periods/powers per object (bestperiods_top_three.txt)
+//   --top3 <file>                  three best periods and powers per object (the paper's
+//                                  bestperiods_top_three.txt layout, PRINTPERIODS 3)
 //   -ppf, --printpgramfile <file>  periodogram to <file> (the paper's pgram.txt layout)
 //   -q, --quiet
 // The data file is the reference's text format: comma-separated object id, time,
-// magnitude[, dmag] per line (source/main.cu:1781-1843). The work is done by
-// LombScarglePy of the matching libpyls*.so next to this executable, so the results
-// are those of the drop-in libraries; its stdout lines and gpu_stats.txt append are
-// the reference's.
+// magnitude[, dmag] per line (source/main.cu:1781-1843).
+//
+// The GPU modes call liblsgb.so (next to this executable) once: the three best frequencies
+// of every object come out of the periodogram kernel itself (lsgb_periodogram_top3_host),
+// and the periodogram is copied to the host only for -ppf. The double build computes in the
+// plain FP64 form, the float build in the mixed form (LSGB_PRECISION=plain|mixed chooses).
+// The CPU modes run the reference's CPU algorithm in the build's type (lsgb_cpu.h), and
+// take the three best from the returned periodogram by the reference's three scans.
 #include <dlfcn.h>
 #include <limits.h>
 #include <stdint.h>
@@ -39,6 +48,13 @@
 #include <string>
 #include <vector>
 
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../../include/lsgb.h"
+#include "lsgb_cpu.h"
+
 namespace {
 
 struct Args {
@@ -47,7 +63,8 @@ struct Args {
     long nfreq = -1;
     int mode = 0;  // in the paper numbering (1, 2, 4, 5)
     int error = -1, dbl = -1;
-    bool print_screen = false, quiet = false;
+    int nthreads = 0;  // 0: the OpenMP default
+    bool print_screen = false, quiet = false, normalize = false;
 };
 
 [[noreturn]] void usage(const char *msg) {
@@ -55,8 +72,9 @@ struct Args {
     fprintf(stderr,
             "usage: lsgb_main <file> <min freq> <max freq> <num freqs> <mode 1|2|4|5> [options]\n"
             "       lsgb_main -f <file> -min <f> -max <f> -fq <n> -m <mode 1-4> [options]\n"
-            "options: -e/--error -d/--double -ps/--printscreen -pf/--printfile <file>\n"
-            "         --top3 <file> -ppf/--printpgramfile <file> -q/--quiet\n");
+            "options: -e/--error -d/--double -nrp/--normpgram -n/--nthreads <k> -ng/--ngpus <k>\n"
+            "         -ps/--printscreen -pf/--printfile <file> --top3 <file>\n"
+            "         -ppf/--printpgramfile <file> -q/--quiet\n");
     exit(2);
 }
 
@@ -99,6 +117,15 @@ Args parse(int argc, char **argv) {
         else if (!strcmp(s, "--top3")) a.top3_file = val(s);
         else if (is(s, "-ppf", "--printpgramfile")) a.pgram_file = val(s);
         else if (is(s, "-q", "--quiet")) a.quiet = true;
+        else if (is(s, "-nrp", "--normpgram")) a.normalize = true;
+        else if (is(s, "-n", "--nthreads")) {
+            a.nthreads = (int)inum(val(s), "threads");
+            if (a.nthreads < 1) usage("the number of threads must be positive");
+        } else if (is(s, "-ng", "--ngpus")) {
+            const long g = inum(val(s), "GPUs");
+            if (g < 1) usage("the number of GPUs must be positive");
+            if (g > 1) fprintf(stderr, "lsgb_main: one GPU is used (-ng %ld ignored)\n", g);
+        }
         else if (s[0] == '-' && !(s[1] >= '0' && s[1] <= '9') && s[1] != '.') usage((std::string("unknown option ") + s).c_str());
         else pos.push_back(s);
     }
@@ -175,97 +202,189 @@ std::string exe_dir() {
     return s.substr(0, s.find_last_of('/'));
 }
 
+// The reference's three scans over one periodogram (source/main.cu:1165-1219): the three
+// largest positive powers at distinct indices, best first, the first index among equal
+// powers; (0, index 0) where there are fewer.
+template <typename T>
+void top3_scan(const T *p, size_t nf, uint32_t idx[3], T pw[3]) {
+    for (int r = 0; r < 3; ++r) {
+        idx[r] = 0;
+        pw[r] = 0;
+        for (size_t k = 0; k < nf; ++k) {
+            const bool taken = (r >= 1 && k == idx[0]) || (r >= 2 && k == idx[1]);
+            if (!taken && pw[r] < p[k]) {
+                pw[r] = p[k];
+                idx[r] = (uint32_t)k;
+            }
+        }
+    }
+}
+
+typedef int (*EngineCreateFn)(int, lsgb_engine **);
+typedef const char *(*LastErrorFn)(void);
+typedef int (*Top3HostFn)(lsgb_engine *, int, int, int, const void *, const void *, const void *,
+                          const uint64_t *, uint32_t, double, double, uint32_t, int, void *,
+                          uint32_t *, void *);
+
 template <typename T>
 int run(const Args &a, Data &d) {
-    const bool err = a.error == 1;
-    const std::string lib = exe_dir() + "/libpyls" + (err ? "error" : "noerror") +
-                            (sizeof(T) == 4 ? "float" : "double") + ".so";
-    void *h = dlopen(lib.c_str(), RTLD_NOW | RTLD_LOCAL);
-    if (!h) {
-        fprintf(stderr, "lsgb_main: %s\n", dlerror());
-        return 1;
-    }
-    typedef void (*Fn)(unsigned *, T *, T *, T *, unsigned, double, double, unsigned, int, T *);
-    typedef int (*StatusFn)();
-    Fn fn = (Fn)dlsym(h, "LombScarglePy");
-    StatusFn st = (StatusFn)dlsym(h, "LombScarglePy_last_status");
-    if (!fn || !st) {
-        fprintf(stderr, "lsgb_main: %s does not export LombScarglePy\n", lib.c_str());
-        return 1;
-    }
+    const bool err = a.error == 1, gpu = a.mode == 1 || a.mode == 2;
     const size_t rows = d.t.size();
     std::vector<T> t(d.t.begin(), d.t.end()), y(d.y.begin(), d.y.end()), dy(d.dy.begin(), d.dy.end());
     // objects: runs of equal ids (source/main.cu:468-510); one object in the single modes
-    std::vector<size_t> start{0};
+    std::vector<uint64_t> offs{0};
     if (a.mode == 1 || a.mode == 4)
         for (size_t i = 1; i < rows; ++i)
-            if (d.id[i] != d.id[i - 1]) start.push_back(i);
-    const size_t nobj = start.size();
+            if (d.id[i] != d.id[i - 1]) offs.push_back(i);
+    offs.push_back(rows);
+    const uint32_t nobj = (uint32_t)offs.size() - 1;
     const size_t nf = (size_t)a.nfreq;
-    std::vector<T> pgram(nobj * nf, T(0));
-    printf("\nDataset file: %s", a.file.c_str());
-    printf("\nData import: Total rows: %zu", rows);
-    const auto t0 = std::chrono::steady_clock::now();
-    fn(d.id.data(), t.data(), y.data(), dy.data(), (unsigned)rows, a.fmin, a.fmax, (unsigned)nf,
-       a.mode, pgram.data());
-    fflush(stdout);
-    const double secs =
-        std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-    if (st() != 0) {
-        fprintf(stderr, "lsgb_main: LombScarglePy failed with status %d\n", st());
-        return 1;
-    }
-    // periods from the periodogram, first maximum from power 0 (source/main.cu:1545-1563)
+    // The reference's drivers take the limits in the build's type (source/main.cu:742, :1358).
     const T fminT = (T)a.fmin, fmaxT = (T)a.fmax;
-    const double step = (double)(T)(((double)fmaxT - (double)fminT) / (nf * 1.0));
-    std::vector<double> per(3 * nobj), pow3(3 * nobj);
-    double sum = 0;
-    for (size_t o = 0; o < nobj; ++o) {
-        const T *p = pgram.data() + o * nf;
-        size_t best[3] = {0, 0, 0};
-        T bp[3] = {0, 0, 0};
-        for (int r = 0; r < 3; ++r)  // three scans, each skipping the earlier maxima (:1165-1219)
-            for (size_t k = 0; k < nf; ++k) {
-                bool skip = false;
-                for (int q = 0; q < r; ++q) skip |= (k == best[q]);
-                if (!skip && bp[r] < p[k]) {
-                    bp[r] = p[k];
-                    best[r] = k;
-                }
-            }
-        for (int r = 0; r < 3; ++r) {
-            per[3 * o + r] = (1.0 / ((double)fminT + best[r] * step)) * 2.0 * M_PI;
-            pow3[3 * o + r] = (double)bp[r];
+    printf("\nDataset file: %s", a.file.c_str());
+    printf("\nMinimum Frequency: %f", a.fmin);
+    printf("\nMaximum Frequency: %f", a.fmax);
+    printf("\nNumber of frequencies to test: %zu", nf);
+    printf("\nMode: %d", a.mode);
+    if (err) printf("\nExecuting L-S variant from AstroPy that propogates error and floats the mean");
+    printf("\nData import: Total rows: %zu", rows);
+    if (a.mode == 1 || a.mode == 4) printf("\nUnique objects in file: %u", nobj);
+    const bool want_pgram = !a.pgram_file.empty();
+    std::vector<T> pgram;
+    std::vector<uint32_t> idx3(3 * (size_t)nobj);
+    std::vector<T> pow3(3 * (size_t)nobj);
+    double step_period = 0;  // GPU modes: the frequency step of the period formula
+    T step_cpu = 0;          // CPU modes: the step in the build's type
+    const auto t0 = std::chrono::steady_clock::now();
+    if (gpu) {
+        const std::string lib = exe_dir() + "/liblsgb.so";
+        void *h = dlopen(lib.c_str(), RTLD_NOW | RTLD_LOCAL);
+        if (!h) {
+            fprintf(stderr, "lsgb_main: %s\n", dlerror());
+            return 1;
         }
-        sum += per[3 * o];
+        auto create = (EngineCreateFn)dlsym(h, "lsgb_engine_create");
+        auto last_error = (LastErrorFn)dlsym(h, "lsgb_last_error");
+        auto top3 = (Top3HostFn)dlsym(h, "lsgb_periodogram_top3_host");
+        if (!create || !last_error || !top3) {
+            fprintf(stderr, "lsgb_main: %s lacks the lsgb_* entry points\n", lib.c_str());
+            return 1;
+        }
+        // the generalized variant centers y per object first (source/main.cu:1045, :187)
+        if (err)
+            for (uint32_t o = 0; o < nobj; ++o)
+                lsgb_cpu::precenter<T>(y.data() + offs[o], dy.data() + offs[o],
+                                       (uint32_t)(offs[o + 1] - offs[o]));
+        int precision = a.dbl ? LSGB_PLAIN_FP64 : LSGB_MIXED;
+        const char *pe = getenv("LSGB_PRECISION");
+        if (pe && !strcmp(pe, "plain")) precision = LSGB_PLAIN_FP64;
+        if (pe && !strcmp(pe, "mixed")) precision = LSGB_MIXED;
+        // the kernels' grid: fmin + k * df, df computed in double and held in the build's
+        // type (source/kernel.cu:517)
+        const double fmin = (double)fminT;
+        const double df = (double)(T)(((double)fmaxT - (double)fminT) / (nf * 1.0));
+        lsgb_engine *eng = nullptr;
+        int rc = create(0, &eng);
+        if (rc == LSGB_OK) {
+            if (want_pgram) pgram.assign((size_t)nobj * nf, T(0));
+            const auto tk = std::chrono::steady_clock::now();
+            rc = top3(eng, err ? LSGB_GENERALIZED : LSGB_STANDARD, precision,
+                      sizeof(T) == 4 ? LSGB_F32 : LSGB_F64, t.data(), y.data(),
+                      err ? dy.data() : nullptr, offs.data(), nobj, fmin, df, (uint32_t)nf,
+                      (!err && a.normalize) ? 1 : 0, want_pgram ? pgram.data() : nullptr,
+                      idx3.data(), pow3.data());
+            printf("\nTime to compute kernel: %f",
+                   std::chrono::duration<double>(std::chrono::steady_clock::now() - tk).count());
+        }
+        if (rc != LSGB_OK) {
+            fprintf(stderr, "lsgb_main: GPU computation failed: %s\n", last_error());
+            return 1;
+        }
+        // the period formula of the GPU drivers uses the step in double (source/main.cu:1140)
+        step_period = ((double)fmaxT - (double)fminT) / (nf * 1.0);
+    } else {
+#ifdef _OPENMP
+        if (a.nthreads > 0) omp_set_num_threads(a.nthreads);
+#endif
+        pgram.assign((size_t)nobj * nf, T(0));
+        const T freqStep = (fmaxT - fminT) / (nf * 1.0);
+        // objects in parallel (MODE 4), or frequencies in parallel within one (MODE 5), as
+        // the reference's CPU modes (source/main.cu:1487, :1617)
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic) if (a.mode == 4)
+#endif
+        for (uint32_t o = 0; o < nobj; ++o) {
+            const uint64_t r0 = offs[o];
+            const uint32_t n = (uint32_t)(offs[o + 1] - r0);
+            T *pg = pgram.data() + (size_t)o * nf;
+            if (err)
+                lsgb_cpu::object_pgram<T, 1>(t.data() + r0, y.data() + r0, dy.data() + r0, n,
+                                             (uint32_t)nf, fminT, freqStep, pg, a.mode == 5, false);
+            else
+                lsgb_cpu::object_pgram<T, 0>(t.data() + r0, y.data() + r0, dy.data() + r0, n,
+                                             (uint32_t)nf, fminT, freqStep, pg, a.mode == 5,
+                                             a.normalize);
+            top3_scan(pg, nf, idx3.data() + 3 * (size_t)o, pow3.data() + 3 * (size_t)o);
+        }
+        step_cpu = freqStep;
     }
+    const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    // period = 2 pi / omega: in double from the double step in the GPU drivers
+    // (source/main.cu:1140-1160), in the build's type in the CPU modes (computePeriod,
+    // source/main.cu:1545-1563)
+    std::vector<double> per(3 * (size_t)nobj);
+    double sum = 0;
+    for (size_t i = 0; i < per.size(); ++i)
+        per[i] = gpu ? (1.0 / ((double)fminT + (idx3[i] * step_period))) * 2.0 * M_PI
+                     : (double)(T)((1.0 / (fminT + (idx3[i] * step_cpu))) * 2.0 * M_PI);
+    for (uint32_t o = 0; o < nobj; ++o) sum += per[3 * (size_t)o];
     const uint32_t single_id = d.id.empty() ? 0 : d.id[0];
-    auto obj_id = [&](size_t o) { return (a.mode == 2 || a.mode == 5) ? single_id : d.id[start[o]]; };
-    if (!a.quiet) printf("\nTotal time: %f", secs);
-    printf("\n[lsgb_main] Sum of periods: %f\n", sum);
+    auto obj_id = [&](uint32_t o) { return (a.mode == 2 || a.mode == 5) ? single_id : d.id[offs[o]]; };
+    if (a.mode == 2) {
+        printf("\nPeriod: %f", per[0]);
+        printf("\nMaximum power at found period: %f", (double)pow3[0]);
+    }
+    if (!a.quiet) printf("\nTotal time to compute batch: %f", secs);
+    if (a.mode == 1 || a.mode == 4)
+        printf("\n[Validation] Sum of all periods: %f\n", sum);
+    else
+        printf("\n[Validation] Period: %f, Power: %f\n", per[0], (double)pow3[0]);
     if (a.print_screen)
-        for (size_t o = 0; o < nobj; ++o)
-            printf("Object: %u Period: %f, Power: %f \n", obj_id(o), per[3 * o], pow3[3 * o]);
+        for (uint32_t o = 0; o < nobj; ++o)
+            printf("Object: %u Period: %f, Power: %f \n", obj_id(o), per[3 * (size_t)o],
+                   (double)pow3[3 * (size_t)o]);
     if (!a.period_file.empty()) {
         std::ofstream f(a.period_file);
         f.precision(6);
-        for (size_t o = 0; o < nobj; ++o) f << obj_id(o) << ", " << per[3 * o] << ", " << pow3[3 * o] << "\n";
+        for (uint32_t o = 0; o < nobj; ++o)
+            f << obj_id(o) << ", " << per[3 * (size_t)o] << ", " << pow3[3 * (size_t)o] << "\n";
     }
     if (!a.top3_file.empty()) {
         std::ofstream f(a.top3_file);
         f.precision(6);
-        for (size_t o = 0; o < nobj; ++o)
-            f << obj_id(o) << ", " << per[3 * o] << ", " << per[3 * o + 1] << ", " << per[3 * o + 2]
-              << ", " << pow3[3 * o] << ", " << pow3[3 * o + 1] << ", " << pow3[3 * o + 2] << "\n";
+        for (uint32_t o = 0; o < nobj; ++o) {
+            const size_t b = 3 * (size_t)o;
+            f << obj_id(o) << ", " << per[b] << ", " << per[b + 1] << ", " << per[b + 2] << ", "
+              << pow3[b] << ", " << pow3[b + 1] << ", " << pow3[b + 2] << "\n";
+        }
     }
-    if (!a.pgram_file.empty()) {
+    if (want_pgram) {
         std::ofstream f(a.pgram_file);
         f.precision(4);
-        for (size_t o = 0; o < nobj; ++o) {
+        for (uint32_t o = 0; o < nobj; ++o) {
             f << obj_id(o) << ", ";
-            for (size_t k = 0; k < nf; ++k) f << pgram[o * nf + k] << ", ";
+            for (size_t k = 0; k < nf; ++k) f << pgram[(size_t)o * nf + k] << ", ";
             f << "\n";
         }
+    }
+    // the reference appends a line per run to gpu_stats.txt in the working directory
+    const char *no = getenv("LSGB_NO_STATS");
+    if (!(no && !strcmp(no, "1"))) {
+        std::ofstream g("gpu_stats.txt", std::ios::app);
+        g << secs << ", " << a.file << ", Sum of periods: " << sum << ", Min/Max Freq: " << a.fmin
+          << "/" << a.fmax << ",  Num tested freq: " << nf << ", MODE: " << a.mode
+          << ", ERROR/DTYPE/ENGINE: " << (err ? 1 : 0) << ", " << (sizeof(T) == 4 ? "float" : "double")
+          << ", lsgb" << std::endl;
     }
     return 0;
 }

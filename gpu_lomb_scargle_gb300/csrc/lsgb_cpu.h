@@ -24,82 +24,91 @@
 
 namespace lsgb_cpu {
 
+// Standard power at angular frequency om. The statement order (and so the rounding, in
+// float and double) is that of the reference's CPU loop: the five sums over the
+// observations, the time shift that decouples the cosine and sine terms, then the two
+// quotients of the tau-rotated form.
 template <typename T>
-T power_std(const T *x, const T *y, uint32_t n, T w) {
-    T c, s, xc = 0.0, xs = 0.0, cc = 0.0, ss = 0.0, cs = 0.0;
+T power_std(const T *x, const T *y, uint32_t n, T om) {
+    T cw, sw, syc = 0.0, sys = 0.0, scc = 0.0, sss = 0.0, scs = 0.0;
     for (uint32_t j = 0; j < n; j++) {
-        c = std::cos(w * x[j]);
-        s = std::sin(w * x[j]);
-        xc += y[j] * c;
-        xs += y[j] * s;
-        cc += c * c;
-        ss += s * s;
-        cs += c * s;
+        cw = std::cos(om * x[j]);
+        sw = std::sin(om * x[j]);
+        syc += y[j] * cw;
+        sys += y[j] * sw;
+        scc += cw * cw;
+        sss += sw * sw;
+        scs += cw * sw;
     }
-    T tau = std::atan2(2.0 * cs, cc - ss) / (2.0 * w);
-    T c_tau = std::cos(w * tau);
-    T s_tau = std::sin(w * tau);
-    T c_tau2 = c_tau * c_tau;
-    T s_tau2 = s_tau * s_tau;
-    T cs_tau = 2.0 * c_tau * s_tau;
-    return 0.5 * ((((c_tau * xc + s_tau * xs) * (c_tau * xc + s_tau * xs)) /
-                   (c_tau2 * cc + cs_tau * cs + s_tau2 * ss)) +
-                  (((c_tau * xs - s_tau * xc) * (c_tau * xs - s_tau * xc)) /
-                   (c_tau2 * ss - cs_tau * cs + s_tau2 * cc)));
+    const T shift = std::atan2(2.0 * scs, scc - sss) / (2.0 * om);
+    const T cr = std::cos(om * shift);
+    const T sr = std::sin(om * shift);
+    const T cr2 = cr * cr;
+    const T sr2 = sr * sr;
+    const T csr = 2.0 * cr * sr;
+    const T along = cr * syc + sr * sys;    // projection on the shifted cosine
+    const T across = cr * sys - sr * syc;   // and on the shifted sine
+    const T quo_c = (along * along) / (cr2 * scc + csr * scs + sr2 * sss);
+    const T quo_s = (across * across) / (cr2 * sss - csr * scs + sr2 * scc);
+    return 0.5 * (quo_c + quo_s);
 }
 
+// Generalized power (floating mean, weights 1/dy^2) at angular frequency om: a first pass
+// for the time shift from the weighted doubled-angle sums, a second at om (t - shift) for the
+// weighted, mean-subtracted sums. Statement order as in the reference's CPU loop.
 template <typename T>
-T power_gen(const T *x, const T *y, const T *dy, uint32_t n, T f) {
-    T w, omega_t, sin_omega_t, cos_omega_t, S = 0.0, C = 0.0, S2 = 0.0, C2 = 0.0, wsum = 0.0;
+T power_gen(const T *x, const T *y, const T *dy, uint32_t n, T om) {
+    T wt, ph, sph, cph, m_s = 0.0, m_c = 0.0, m_s2 = 0.0, m_c2 = 0.0, wsum = 0.0;
     for (uint32_t j = 0; j < n; j++) {
-        w = 1.0 / dy[j];
-        w *= w;
-        wsum += w;
-        omega_t = f * x[j];
-        sin_omega_t = std::sin(omega_t);
-        cos_omega_t = std::cos(omega_t);
-        S += w * sin_omega_t;
-        C += w * cos_omega_t;
-        S2 += 2.0 * w * sin_omega_t * cos_omega_t;
-        C2 += w - 2.0 * w * sin_omega_t * sin_omega_t;
+        wt = 1.0 / dy[j];
+        wt *= wt;
+        wsum += wt;
+        ph = om * x[j];
+        sph = std::sin(ph);
+        cph = std::cos(ph);
+        m_s += wt * sph;
+        m_c += wt * cph;
+        m_s2 += 2.0 * wt * sph * cph;
+        m_c2 += wt - 2.0 * wt * sph * sph;
     }
-    S2 /= wsum;
-    C2 /= wsum;
-    S /= wsum;
-    C /= wsum;
-    S2 -= (2.0 * S * C);
-    C2 -= (C * C - S * S);
-    T tau = 0.5 * std::atan2(S2, C2) / f;
-    T Y = 0.0, YY = 0.0, Stau = 0.0, Ctau = 0.0, YCtau = 0.0, YStau = 0.0, CCtau = 0.0, SStau = 0.0;
+    m_s2 /= wsum;
+    m_c2 /= wsum;
+    m_s /= wsum;
+    m_c /= wsum;
+    m_s2 -= (2.0 * m_s * m_c);
+    m_c2 -= (m_c * m_c - m_s * m_s);
+    const T shift = 0.5 * std::atan2(m_s2, m_c2) / om;
+    T my = 0.0, myy = 0.0, ms = 0.0, mc = 0.0, myc = 0.0, mys = 0.0, mcc = 0.0, mss = 0.0;
     for (uint32_t j = 0; j < n; j++) {
-        w = 1.0 / dy[j];
-        w *= w;
-        omega_t = f * (x[j] - tau);
-        sin_omega_t = std::sin(omega_t);
-        cos_omega_t = std::cos(omega_t);
-        Y += w * y[j];
-        YY += w * y[j] * y[j];
-        Ctau += w * cos_omega_t;
-        Stau += w * sin_omega_t;
-        YCtau += w * y[j] * cos_omega_t;
-        YStau += w * y[j] * sin_omega_t;
-        CCtau += w * cos_omega_t * cos_omega_t;
-        SStau += w * sin_omega_t * sin_omega_t;
+        wt = 1.0 / dy[j];
+        wt *= wt;
+        ph = om * (x[j] - shift);
+        sph = std::sin(ph);
+        cph = std::cos(ph);
+        my += wt * y[j];
+        myy += wt * y[j] * y[j];
+        mc += wt * cph;
+        ms += wt * sph;
+        myc += wt * y[j] * cph;
+        mys += wt * y[j] * sph;
+        mcc += wt * cph * cph;
+        mss += wt * sph * sph;
     }
-    Y /= wsum;
-    YY /= wsum;
-    Ctau /= wsum;
-    Stau /= wsum;
-    YCtau /= wsum;
-    YStau /= wsum;
-    CCtau /= wsum;
-    SStau /= wsum;
-    YCtau -= Y * Ctau;
-    YStau -= Y * Stau;
-    CCtau -= Ctau * Ctau;
-    SStau -= Stau * Stau;
-    YY -= Y * Y;
-    return (YCtau * YCtau / CCtau + YStau * YStau / SStau) / YY;
+    my /= wsum;
+    myy /= wsum;
+    mc /= wsum;
+    ms /= wsum;
+    myc /= wsum;
+    mys /= wsum;
+    mcc /= wsum;
+    mss /= wsum;
+    // covariances about the weighted means
+    myc -= my * mc;
+    mys -= my * ms;
+    mcc -= mc * mc;
+    mss -= ms * ms;
+    myy -= my * my;
+    return (myc * myc / mcc + mys * mys / mss) / myy;
 }
 
 // y -= sum(w*y)/sum(w), w = 1/sqrt(dy), in place; sums kept in DTYPE as the
@@ -139,10 +148,12 @@ void argmax(const T *p, uint32_t nf, T minFreq, T freqStep, T *period, T *power)
     *power = maxPower;
 }
 
-// One object's full periodogram into pg[0..nf), normalized for the standard variant.
+// One object's full periodogram into pg[0..nf); the standard variant is normalized by
+// 2/(N var(y)) when `normalize` (the Python builds, -DNORMALIZEPGRAM=1; the command line
+// leaves it unnormalized unless asked, source/params.h:40).
 template <typename T, int ERR>
 void object_pgram(const T *x, T *y, const T *dy, uint32_t n, uint32_t nf, T minFreq, T freqStep,
-                  T *pg, bool parallel_freqs) {
+                  T *pg, bool parallel_freqs, bool normalize = true) {
     if (ERR) precenter(y, dy, n);
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static) if (parallel_freqs)
@@ -151,7 +162,7 @@ void object_pgram(const T *x, T *y, const T *dy, uint32_t n, uint32_t nf, T minF
         T f = minFreq + (freqStep * i);
         pg[i] = ERR ? power_gen<T>(x, y, dy, n, f) : power_std<T>(x, y, n, f);
     }
-    if (!ERR) {
+    if (!ERR && normalize) {
         const double scale = 2.0 / (n * var_pop(y, n));
         for (uint32_t j = 0; j < nf; j++) pg[j] *= scale;
     }
@@ -160,7 +171,7 @@ void object_pgram(const T *x, T *y, const T *dy, uint32_t n, uint32_t nf, T minF
 // MODE 4: objects are runs of equal id; returns the sum of the best periods.
 template <typename T, int ERR>
 double batch(const uint32_t *ids, const T *x, T *y, const T *dy, uint32_t rows, T minFreq, T maxFreq,
-             uint32_t nf, T *pgram, uint32_t *n_obj_out) {
+             uint32_t nf, T *pgram, uint32_t *n_obj_out, bool normalize = true) {
     std::vector<uint32_t> start{0};
     for (uint32_t i = 1; i < rows; i++)
         if (ids[i] != ids[i - 1]) start.push_back(i);
@@ -175,7 +186,7 @@ double batch(const uint32_t *ids, const T *x, T *y, const T *dy, uint32_t rows, 
     for (uint32_t o = 0; o < nobj; o++) {
         const uint32_t a = start[o], n = start[o + 1] - start[o];
         T *pg = pgram + (uint64_t)o * nf;
-        object_pgram<T, ERR>(x + a, y + a, dy + a, n, nf, minFreq, freqStep, pg, false);
+        object_pgram<T, ERR>(x + a, y + a, dy + a, n, nf, minFreq, freqStep, pg, false, normalize);
         argmax(pg, nf, minFreq, freqStep, &period[o], &power[o]);
     }
     double sum = 0;
@@ -186,9 +197,9 @@ double batch(const uint32_t *ids, const T *x, T *y, const T *dy, uint32_t rows, 
 // MODE 5: all rows are one object.
 template <typename T, int ERR>
 void single(const T *x, T *y, const T *dy, uint32_t rows, T minFreq, T maxFreq, uint32_t nf,
-            T *pgram, T *period, T *power) {
+            T *pgram, T *period, T *power, bool normalize = true) {
     const T freqStep = (maxFreq - minFreq) / (nf * 1.0);
-    object_pgram<T, ERR>(x, y, dy, rows, nf, minFreq, freqStep, pgram, true);
+    object_pgram<T, ERR>(x, y, dy, rows, nf, minFreq, freqStep, pgram, true, normalize);
     argmax(pgram, nf, minFreq, freqStep, period, power);
 }
 
