@@ -54,8 +54,8 @@ TENSOR_FLOPS_PER_PAIR_STD = 48
 # lane-ops for 12 pairs
 CUDA_CORE_SHAPE_STD = (12, 256, 2, 2, 0)
 OPS_PER_PAIR_CUDA_CORE = 76 / 12
-# DRAM read + write bytes of one tensor-kernel launch, from the ncu capture of the same
-# batch at 1e5 frequencies (profiles/tensor_kernel_std_999obj_1e5freq.md): the operand
+# DRAM read + write bytes of one tensor-kernel launch, from an ncu capture of the same
+# batch at 1e5 frequencies (dram__bytes_read.sum + dram__bytes_write.sum): the operand
 # table (32 KB of split-FP16 left operands per K-block, 11,487 K-blocks: 376 MB) is read
 # from DRAM once per launch whatever the grid size, because the units of one object run
 # back to back and re-read it from L2; nothing is written without a periodogram

@@ -22,7 +22,8 @@ LSGB_SYMBOLS = ("lsgb_engine_create", "lsgb_engine_destroy", "lsgb_last_error", 
                 "lsgb_get_tuning", "lsgb_periodogram_noalloc", "lsgb_server_create",
                 "lsgb_server_submit", "lsgb_server_poll", "lsgb_server_stats", "lsgb_server_now",
                 "lsgb_server_destroy", "lsgb_set_reanchor", "lsgb_fp64_sincos_check", "lsgb_plan_create",
-                "lsgb_plan_launch", "lsgb_plan_info", "lsgb_plan_destroy")
+                "lsgb_plan_launch", "lsgb_plan_info", "lsgb_plan_destroy", "lsgb_plan_status_async",
+                "lsgb_status_async", "lsgb_set_wait_limit")
 PYABI_SYMBOLS = ("LombScarglePy", "LombScarglePy_last_status")
 
 
@@ -108,5 +109,11 @@ def lsgb() -> ctypes.CDLL:
         lib.lsgb_plan_info.restype = i32
         lib.lsgb_plan_destroy.argtypes = [vp]
         lib.lsgb_plan_destroy.restype = None
+        lib.lsgb_plan_status_async.argtypes = [vp, c.POINTER(c.c_uint32), vp]
+        lib.lsgb_plan_status_async.restype = i32
+        lib.lsgb_status_async.argtypes = [vp, c.POINTER(c.c_uint32), vp]
+        lib.lsgb_status_async.restype = i32
+        lib.lsgb_set_wait_limit.argtypes = [vp, c.c_uint64]
+        lib.lsgb_set_wait_limit.restype = i32
         lib._lsgb_typed = True
     return lib

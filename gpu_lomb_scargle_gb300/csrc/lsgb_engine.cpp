@@ -84,8 +84,9 @@ void two_prod(double a, double b_hi, double b_lo, double &hi, double &lo) {
 struct Workspace {
     DevBuf objs, offs, perm, rec, tile_best, counter, keys;
     DevBuf optab;  // tensor form: per-K-block left operands and steps (tensor_optab_bytes)
-    // sticky error word of the tensor-form kernel (a bounded pipeline wait that timed
-    // out); zeroed when allocated and after it is reported
+    // sticky status word of the call's kernels (kStatusTimeout: a bounded pipeline wait of
+    // the tensor form ran out; kStatusBadInput: non-finite or invalid inputs); zeroed when
+    // allocated and after it is reported
     DevBuf status;
     void release() {
         DevBuf *b[] = {&objs, &offs, &perm, &rec, &tile_best, &counter, &keys, &optab, &status};
@@ -108,6 +109,7 @@ struct Batch {
     uint32_t reanchor = 0;
     bool want_best = false, fold = false;
     uint32_t top = 1;  // best frequencies per object: 1 (argmax) or 3 (the top three)
+    long long wait_cycles = 0;  // tensor form: bounded-wait limit (0: the kernel's default)
     size_t smem = 0;
     int grid = 0;
     uint32_t kernels = 0;
@@ -248,7 +250,7 @@ int upload_tables(const Batch &b, Workspace &ws, cudaStream_t st) {
         LSGB_CUDA(ws.keys.ensure(sizeof(unsigned long long) * b.n_obj * b.top));
     if (mixed) LSGB_CUDA(ws.rec.ensure(mixed_global_rec_bytes(b.shape) * b.rows));
     if (mixed && b.shape.x2 == 3) LSGB_CUDA(ws.optab.ensure(tensor_optab_bytes(b.variant, b.total_kb)));
-    if (mixed && !ws.status.p) {
+    if (!ws.status.p) {
         LSGB_CUDA(ws.status.ensure(sizeof(uint32_t)));
         LSGB_CUDA(cudaMemsetAsync(ws.status.p, 0, sizeof(uint32_t), st));
     }
@@ -261,16 +263,40 @@ int upload_tables(const Batch &b, Workspace &ws, cudaStream_t st) {
     return LSGB_OK;
 }
 
-// Reports (and clears) a pipeline-wait timeout recorded by the tensor-form kernel. Call
-// after the work that may have set it has completed.
+// The status a status word stands for (0: none).
+int status_code(uint32_t v) {
+    if (v & kStatusBadInput)
+        return fail(LSGB_ERR_INVALID,
+                    "invalid input: a non-finite time or magnitude, or (generalized variant) a "
+                    "non-finite or non-positive dmag; the results of the call are invalid");
+    if (v & kStatusTimeout)
+        return fail(LSGB_ERR_CUDA,
+                    "tensor-form kernel: a pipeline wait timed out; the results of the call are invalid");
+    return LSGB_OK;
+}
+
+// Reports (and clears) what the call's kernels recorded in the status word. Call after the
+// work that may have set it has completed.
 int check_status(Workspace &ws) {
     if (!ws.status.p) return LSGB_OK;
     uint32_t v = 0;
     LSGB_CUDA(cudaMemcpy(&v, ws.status.p, sizeof(v), cudaMemcpyDeviceToHost));
     if (v == 0) return LSGB_OK;
     LSGB_CUDA(cudaMemset(ws.status.p, 0, sizeof(uint32_t)));
-    return fail(LSGB_ERR_CUDA,
-                "tensor-form kernel: a pipeline wait timed out; the results of the call are invalid");
+    return status_code(v);
+}
+
+// Queues on st a copy of the status word to host memory and then its reset, so that the
+// caller learns, once st has reached this point, what the work before it recorded.
+int status_async(Workspace &ws, uint32_t *host, cudaStream_t st) {
+    if (!host) return fail(LSGB_ERR_INVALID, "status destination is NULL");
+    if (!ws.status.p) {
+        *host = 0;
+        return LSGB_OK;
+    }
+    LSGB_CUDA(cudaMemcpyAsync(host, ws.status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    LSGB_CUDA(cudaMemsetAsync(ws.status.p, 0, sizeof(uint32_t), st));
+    return LSGB_OK;
 }
 
 // Records `ev` on `st`; while `st` is being captured the record becomes an event node
@@ -290,8 +316,8 @@ int enqueue_batch(Batch &b, Workspace &ws, cudaStream_t st, cudaEvent_t ev0, cud
     LSGB_CUDA(cudaMemsetAsync(ws.counter.p, 0, sizeof(uint32_t), st));
     if (b.want_best && mixed)
         LSGB_CUDA(cudaMemsetAsync(ws.keys.p, 0, sizeof(unsigned long long) * b.n_obj * b.top, st));
-    LSGB_CUDA(launch_stats(b.variant, mixed ? 1 : 0, b.dtype, b.normalize, b.y, b.dy, d_objs,
-                           b.n_obj, st));
+    LSGB_CUDA(launch_stats(b.variant, mixed ? 1 : 0, b.dtype, b.normalize, b.t, b.y, b.dy, d_objs,
+                           b.n_obj, (uint32_t *)ws.status.p, st));
     ++kernels;
     if (mixed) {
         GridTurns g;
@@ -320,6 +346,7 @@ int enqueue_batch(Batch &b, Workspace &ws, cudaStream_t st, cudaEvent_t ev0, cud
         a.fold = b.fold ? 1u : 0u;
         a.status = (uint32_t *)ws.status.p;
         a.top = b.top;
+        a.wait_cycles = b.wait_cycles;
         if (b.shape.x2 == 3) {
             LSGB_CUDA(launch_tensor_optab(b.variant, a, b.total_kb, st));
             ++kernels;
@@ -385,6 +412,7 @@ struct lsgb_engine {
     cudaEvent_t ev_main0 = nullptr, ev_main1 = nullptr;  // around the last main-kernel launch
     bool ev_valid = false;
     uint32_t reanchor = 0;  // mixed form: 0 = anchor at each thread's frequency run
+    long long wait_cycles = 0;  // lsgb_set_wait_limit
 };
 
 // A batch whose device work is captured once in a CUDA graph and replayed.
@@ -530,6 +558,7 @@ static int periodogram_device(lsgb_engine *eng, int variant, int precision, int 
                         offsets, n_obj, fmin, df, n_freq, normalize, pgram, best_idx, best_power,
                         top);
     if (rc != LSGB_OK || b.empty) return rc;
+    b.wait_cycles = eng->wait_cycles;
     rc = upload_tables(b, eng->ws, st);
     if (rc != LSGB_OK) return rc;
     rc = enqueue_batch(b, eng->ws, st, eng->ev_main0, eng->ev_main1);
@@ -586,6 +615,7 @@ LSGB_API int lsgb_plan_create(lsgb_engine *eng, int variant, int precision, int 
                         dy, offsets, n_obj, fmin, df, n_freq, normalize, pgram, best_idx,
                         best_power);
     cudaError_t e = cudaSuccess;
+    p->b.wait_cycles = eng->wait_cycles;
     if (rc == LSGB_OK) {
         e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreate(&p->ev0);
@@ -633,7 +663,27 @@ LSGB_API int lsgb_plan_info(lsgb_plan *p, uint32_t *kernels, uint64_t *units, fl
         if (!p->launched) return fail(LSGB_ERR_INVALID, "lsgb_plan_info: plan never launched");
         LSGB_CUDA(cudaEventSynchronize(p->ev1));
         LSGB_CUDA(cudaEventElapsedTime(last_kernel_ms, p->ev0, p->ev1));
+        return check_status(p->ws);  // set by kernels that ran before ev1
     }
+    return LSGB_OK;
+}
+
+LSGB_API int lsgb_plan_status_async(lsgb_plan *p, uint32_t *host_status, void *stream) {
+    if (!p) return fail(LSGB_ERR_INVALID, "lsgb_plan_status_async: plan is NULL");
+    LSGB_CUDA(cudaSetDevice(p->device));
+    return status_async(p->ws, host_status, (cudaStream_t)stream);
+}
+
+LSGB_API int lsgb_status_async(lsgb_engine *eng, uint32_t *host_status, void *stream) {
+    if (!eng) return fail(LSGB_ERR_INVALID, "lsgb_status_async: engine is NULL");
+    LSGB_CUDA(cudaSetDevice(eng->device));
+    return status_async(eng->ws, host_status, (cudaStream_t)stream);
+}
+
+LSGB_API int lsgb_set_wait_limit(lsgb_engine *eng, uint64_t cycles) {
+    if (!eng) return fail(LSGB_ERR_INVALID, "lsgb_set_wait_limit: engine is NULL");
+    if (cycles > (1ull << 40)) return fail(LSGB_ERR_INVALID, "lsgb_set_wait_limit: above 2^40 cycles");
+    eng->wait_cycles = (long long)cycles;
     return LSGB_OK;
 }
 

@@ -94,13 +94,14 @@ struct MixedArgs {
                                    // to use tile_best; zero means "no positive power"
     uint32_t fold;         // 1: shared memory holds a second-level sum area after the records
                            // (objects longer than `chunk` fold their chunk sums into it)
-    uint32_t *status;      // tensor form: bit 0 set when a bounded pipeline wait timed out
-                           // (may be null)
+    uint32_t *status;      // tensor form: kStatusTimeout is set when a bounded pipeline wait
+                           // ran out (may be null)
     const void *optab;     // tensor form: the operand table's A matrices, and
     const void *steps;     // the K-blocks' steps arrays (tensor_step_bytes each); both
                            // filled by launch_tensor_optab for this batch
     uint32_t total_kb;     // tensor form: K-blocks of the batch (the table's phase stride)
     uint32_t top;          // best frequencies kept per object: 1 (argmax) or 3
+    long long wait_cycles; // tensor form: limit of a bounded pipeline wait (0: the default)
 };
 
 
@@ -136,8 +137,14 @@ inline size_t mixed_fold_bytes(int variant, const MixedShape &s) {
 }
 
 // ---- launchers (lsgb_kernels.cu); all asynchronous on `st` ----
-cudaError_t launch_stats(int variant, int mixed, int dtype, int normalize, const void *y,
-                         const void *dy, ObjInfo *objs, uint32_t n_obj, cudaStream_t st);
+// Bits of the status word a call's kernels set (MixedArgs::status, launch_stats).
+constexpr uint32_t kStatusTimeout = 1u;   // a bounded pipeline wait of the tensor form ran out
+constexpr uint32_t kStatusBadInput = 2u;  // a non-finite t / y, or a non-finite or non-positive
+                                          // dy (generalized variant)
+// Per-object statistics; when status is non-null it also checks the inputs (kStatusBadInput).
+cudaError_t launch_stats(int variant, int mixed, int dtype, int normalize, const void *t,
+                         const void *y, const void *dy, ObjInfo *objs, uint32_t n_obj,
+                         uint32_t *status, cudaStream_t st);
 // so_stride 0: ObsRec records whose (cd, sd) step is one grid point (the rotation loops;
 // the tensor form reads only a, b, v0, v1); > 0: SoRec records for a
 // second-order shape whose CTA has so_stride threads. `rec` holds rows x 32 or rows x 96

@@ -133,12 +133,27 @@ __device__ float pow2_scale(double m) {
     return (float)ldexp(1.0, -e);
 }
 
-__global__ void stats_kernel(int variant, int mixed, int dtype, int normalize, const void *y,
-                             const void *dy, ObjInfo *objs) {
+__global__ void stats_kernel(int variant, int mixed, int dtype, int normalize, const void *t,
+                             const void *y, const void *dy, ObjInfo *objs, uint32_t *status) {
     __shared__ double s_red[32];
     ObjInfo &ob = objs[blockIdx.x];
     const uint64_t r0 = ob.row0;
     const uint32_t n = ob.n;
+    // Inputs the algorithm has no answer for: a non-finite time or magnitude, and for the
+    // generalized variant a non-finite or non-positive dmag (weight 1/dmag^2). The
+    // reference computes NaN or infinite powers from them; here the call reports them
+    // (status bit 1, kStatusBadInput) and its results for that object mean nothing.
+    if (status) {
+        bool bad = false;
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+            bad |= !isfinite(load_in(dtype, t, r0 + i)) || !isfinite(load_in(dtype, y, r0 + i));
+            if (variant) {
+                const double e = load_in(dtype, dy, r0 + i);
+                bad |= !(isfinite(e) && e > 0.0);
+            }
+        }
+        if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(status, kStatusBadInput);
+    }
     if (variant == 0) {
         double s = 0.0;
         for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) s += load_in(dtype, y, r0 + i);
@@ -1034,10 +1049,11 @@ cudaError_t occ_mixed_t(int dtype, size_t smem, int *blocks) {
 
 }  // namespace
 
-cudaError_t launch_stats(int variant, int mixed, int dtype, int normalize, const void *y,
-                         const void *dy, ObjInfo *objs, uint32_t n_obj, cudaStream_t st) {
+cudaError_t launch_stats(int variant, int mixed, int dtype, int normalize, const void *t,
+                         const void *y, const void *dy, ObjInfo *objs, uint32_t n_obj,
+                         uint32_t *status, cudaStream_t st) {
     if (n_obj == 0) return cudaSuccess;
-    stats_kernel<<<n_obj, 256, 0, st>>>(variant, mixed, dtype, normalize, y, dy, objs);
+    stats_kernel<<<n_obj, 256, 0, st>>>(variant, mixed, dtype, normalize, t, y, dy, objs, status);
     return cudaGetLastError();
 }
 

@@ -175,7 +175,8 @@ extern "C" LSGB_API int lsgb_periodogram_noalloc(int variant, int dtype, const v
     // the host tables are consumed once the copies above have run
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail_cuda("cudaStreamSynchronize", e);
 
-    if ((e = launch_stats(variant, 1, dtype, normalize, y, dy, d_objs, n_obj, st)) != cudaSuccess)
+    if ((e = launch_stats(variant, 1, dtype, normalize, t, y, dy, d_objs, n_obj, nullptr, st)) !=
+        cudaSuccess)
         return fail_cuda("statistics kernel", e);
     GridTurns g;
     two_prod(fmin, g.f0_hi, g.f0_lo);

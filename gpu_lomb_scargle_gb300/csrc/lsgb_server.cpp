@@ -102,7 +102,7 @@ struct Slot {
     std::vector<Pending> objs;
     std::vector<uint64_t> offsets;
     Pinned<double> h_t, h_y, h_dy, h_power;
-    Pinned<uint32_t> h_idx;
+    Pinned<uint32_t> h_idx, h_status;  // h_status: the batch's status word (LSGB_STATUS_*)
     DevBuf d_t, d_y, d_dy, d_idx, d_power;
 };
 
@@ -136,6 +136,17 @@ size_t batch_footprint(const lsgb_server *s, size_t rows, size_t objs) {
 void publish(lsgb_server *s, Slot &sl) {
     const double t = now_s();
     std::lock_guard<std::mutex> lk(s->mu);
+    if (sl.h_status.p[0] != 0) {
+        // the batch's results are invalid: stop with an error instead of publishing them
+        s->error = sl.h_status.p[0] & LSGB_STATUS_BAD_INPUT
+                       ? "server: a submitted object has a non-finite t / y or an invalid dy"
+                       : "server: a pipeline wait of the tensor-form kernel timed out";
+        s->stop = true;
+        s->inflight_bytes -= sl.footprint;
+        sl.busy = false;
+        sl.objs.clear();
+        return;
+    }
     for (size_t i = 0; i < sl.objs.size(); ++i)
         s->done.push_back(Done{sl.objs[i].id, sl.h_idx.p[i], sl.h_power.p[i], sl.objs[i].t_submit, t});
     s->objects_done += sl.objs.size();
@@ -150,7 +161,8 @@ std::string launch(lsgb_server *s, Slot &sl) {
     size_t rows = 0;
     for (auto &o : sl.objs) rows += o.t.size();
     if (!sl.h_t.ensure(rows) || !sl.h_y.ensure(rows) || !sl.h_dy.ensure(rows) ||
-        !sl.h_idx.ensure(n_obj) || !sl.h_power.ensure(n_obj) || !sl.d_t.ensure(8 * rows) ||
+        !sl.h_idx.ensure(n_obj) || !sl.h_power.ensure(n_obj) || !sl.h_status.ensure(1) ||
+        !sl.d_t.ensure(8 * rows) ||
         !sl.d_y.ensure(8 * rows) || !sl.d_dy.ensure(8 * rows) || !sl.d_idx.ensure(4 * n_obj) ||
         !sl.d_power.ensure(8 * n_obj))
         return "server: staging allocation failed";
@@ -176,6 +188,9 @@ std::string launch(lsgb_server *s, Slot &sl) {
     if (rc != LSGB_OK) return std::string("server: ") + lsgb_last_error();
     cudaMemcpyAsync(sl.h_idx.p, sl.d_idx.p, 4 * n_obj, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(sl.h_power.p, sl.d_power.p, 8 * n_obj, cudaMemcpyDeviceToHost, st);
+    // what the batch's kernels recorded arrives with its results; publish() checks it
+    if (lsgb_status_async(sl.eng, sl.h_status.p, (void *)st) != LSGB_OK)
+        return std::string("server: ") + lsgb_last_error();
     if (cudaEventRecord(sl.done, st) != cudaSuccess) return "server: cudaEventRecord failed";
     return "";
 }

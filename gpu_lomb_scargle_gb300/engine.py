@@ -14,6 +14,7 @@ import numpy as np
 from . import _native
 
 STANDARD, GENERALIZED = 0, 1
+STATUS_TIMEOUT, STATUS_BAD_INPUT = 1, 2
 PLAIN_FP64, MIXED = 0, 1
 F32, F64 = 0, 1
 
@@ -92,6 +93,22 @@ class Engine:
         self._check(self._lib.lsgb_fp64_sincos_check(self._h, int(n), float(scale),
                                                      ctypes.byref(out)))
         return float(out.value)
+
+    def set_wait_limit(self, cycles: int):
+        """Limit of the tensor form's bounded pipeline waits in SM cycles (0: default)."""
+        self._check(self._lib.lsgb_set_wait_limit(self._h, int(cycles)))
+
+    def status(self, stream=None) -> int:
+        """LSGB_STATUS_* bits recorded by the device calls queued on `stream` so far (waits
+        for the stream), and resets them."""
+        import torch
+
+        st = stream if stream is not None else torch.cuda.current_stream()
+        out = ctypes.c_uint32(0)
+        self._check(self._lib.lsgb_status_async(self._h, ctypes.byref(out),
+                                                ctypes.c_void_p(st.cuda_stream)))
+        st.synchronize()
+        return int(out.value)
 
     def set_reanchor(self, interval: int):
         self._check(self._lib.lsgb_set_reanchor(self._h, int(interval)))

@@ -38,6 +38,12 @@ extern "C" {
 #define LSGB_ERR_NOMEM (-3)     /* device or pinned allocation failed */
 #define LSGB_ERR_NODEVICE (-4)  /* no CUDA device: the engine never computes on the CPU */
 
+/* bits of a call's status word (lsgb_status_async, lsgb_plan_status_async); the host-buffer
+ * calls report them as LSGB_ERR_INVALID / LSGB_ERR_CUDA themselves */
+#define LSGB_STATUS_TIMEOUT 1u    /* a bounded pipeline wait of the tensor form ran out */
+#define LSGB_STATUS_BAD_INPUT 2u  /* a non-finite t or y, or (LSGB_GENERALIZED) a non-finite
+                                     or non-positive dy: no defined periodogram */
+
 /* variant: the reference's ERROR compile flag (source/params.h:12-16) */
 #define LSGB_STANDARD 0     /* ERROR=0: standard L-S, source/kernel.cu:484-631 */
 #define LSGB_GENERALIZED 1  /* ERROR=1: floating mean + 1/dy^2 weights, source/kernel.cu:368-477 */
@@ -80,9 +86,18 @@ LSGB_API int lsgb_periodogram_device(lsgb_engine *eng, int variant, int precisio
                                      double df, uint32_t n_freq, int normalize, void *pgram,
                                      uint32_t *best_idx, void *best_power, void *stream);
 
+/* What the kernels of the device calls queued on `stream` so far have recorded: queues a
+ * copy of the engine's status word into *host_status (host memory, pinned for a truly
+ * asynchronous copy) followed by its reset. Once the stream has reached that point,
+ * *host_status holds LSGB_STATUS_* bits; nonzero means the results of those calls are
+ * invalid. The reference has no counterpart (it exits the process on any CUDA error,
+ * source/main.cu:38-46, and never checks its inputs). */
+LSGB_API int lsgb_status_async(lsgb_engine *eng, uint32_t *host_status, void *stream);
+
 /* The same with host buffers (pinned or pageable). Copies the inputs in, computes,
  * copies pgram (if non-NULL) and the best index/power (if non-NULL) out, and
- * returns when they are in host memory. */
+ * returns when they are in host memory. A status bit recorded by the call's kernels is
+ * returned as LSGB_ERR_INVALID (LSGB_STATUS_BAD_INPUT) or LSGB_ERR_CUDA (timeout). */
 LSGB_API int lsgb_periodogram_host(lsgb_engine *eng, int variant, int precision, int dtype,
                                    const void *t, const void *y, const void *dy,
                                    const uint64_t *offsets, uint32_t n_obj, double fmin, double df,
@@ -130,9 +145,12 @@ LSGB_API int lsgb_plan_create(lsgb_engine *eng, int variant, int precision, int 
                               void *best_power, lsgb_plan **out);
 LSGB_API int lsgb_plan_launch(lsgb_plan *plan, void *stream);
 /* Kernels per launch, work units, and the main kernel's time in the last launch
- * (waits for it; pass NULL to skip). */
+ * (waits for it and then reports a recorded status bit as lsgb_periodogram_host does;
+ * pass NULL to skip). */
 LSGB_API int lsgb_plan_info(lsgb_plan *plan, uint32_t *kernels, uint64_t *units,
                             float *last_kernel_ms);
+/* lsgb_status_async for the launches of a plan. */
+LSGB_API int lsgb_plan_status_async(lsgb_plan *plan, uint32_t *host_status, void *stream);
 LSGB_API void lsgb_plan_destroy(lsgb_plan *plan);
 
 /* Tuning of the mixed kernel: frequencies per thread (F), threads per CTA, the
@@ -226,6 +244,14 @@ LSGB_API int lsgb_set_reanchor(lsgb_engine *eng, uint32_t interval);
 
 /* The shape the engine uses for a variant, in the same 6-int layout. */
 LSGB_API int lsgb_get_tuning(lsgb_engine *eng, int variant, int *out6);
+
+/* Limit, in SM clock cycles, of every bounded pipeline wait of the tensor form (0: the
+ * default, 2^32 cycles, about 2 s). For tests and diagnostics: a limit far below a stage's
+ * time makes the waits run out, and the call then reports LSGB_STATUS_TIMEOUT. The kernel
+ * always waits with the default limit for its own copies and MMAs in flight before it
+ * releases its shared memory and TMEM, whatever this limit. Plans keep the limit they were
+ * created with. */
+LSGB_API int lsgb_set_wait_limit(lsgb_engine *eng, uint64_t cycles);
 
 /* Launch statistics of the last call: kernels launched and the work units the
  * persistent kernel processed. */

@@ -1,7 +1,7 @@
 """Generate the golden fixtures in tests/golden/ from the reference's own CPU path.
 
-Run in a checkout that has the reference at /root/reference and its CPU libraries
-built by ``make -C oracle ref`` (oracle/_ref/libpyls*.so):
+Run where the reference checkout is present (LSGB_REFERENCE_DIR, default /root/reference)
+and its CPU libraries are built by ``make -C oracle ref`` (oracle/_ref/libpyls*.so):
 
     python tests/golden/make_golden.py
 
@@ -26,7 +26,7 @@ ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 from gpu_lomb_scargle_gb300 import synth  # noqa: E402
 
-REF = Path("/root/reference")
+REF = Path(os.environ.get("LSGB_REFERENCE_DIR", "/root/reference"))
 REF_LIB = ROOT / "oracle" / "_ref"
 OUT = Path(__file__).resolve().parent
 TWO_PI = 2.0 * np.pi
