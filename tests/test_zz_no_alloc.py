@@ -26,11 +26,11 @@ from tests.gpu_helpers import MIXED_ATOL, mixed_abs_err
 
 
 def _noalloc(lib, variant, t, y, dy, offsets, fmin, df, n_freq, normalize, pgram, best_idx,
-             best_power, stream):
+             best_power, stream, dtype=E.F64):
     ptr = lambda x: ctypes.c_void_p(x.data_ptr()) if x is not None else None
     offs = np.ascontiguousarray(offsets, dtype=np.uint64)
     return lib.lsgb_periodogram_noalloc(
-        int(variant), E.F64, ptr(t), ptr(y), ptr(dy),
+        int(variant), dtype, ptr(t), ptr(y), ptr(dy),
         offs.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), offs.size - 1, float(fmin),
         float(df), int(n_freq), int(normalize), ptr(pgram), ptr(best_idx), ptr(best_power),
         ctypes.c_void_p(stream.cuda_stream))
@@ -77,6 +77,54 @@ def test_noalloc_matches_regular_entry_point_twice(native_libs, cuda_ok, variant
         diff = bi_n != bi_r
         assert np.all(np.abs(pg_r[rows, bi_r] - pg_r[rows, bi_n])[diff] <= MIXED_ATOL)
         assert np.array_equal(bi_n, np.argmax(pg_n, axis=1))
+    eng.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype", [E.F32, E.F64])
+def test_noalloc_float_inputs_and_long_objects(native_libs, cuda_ok, dtype):
+    """Float and double inputs, and objects longer than one shared-memory chunk of
+    observations (1,024), up to near the 131,072-observation limit: such objects are summed
+    in two levels, as the regular entry point sums them. Two calls in a row again."""
+    import torch
+
+    lib = _native.lsgb()
+    eng = E.Engine(0)
+    dev = torch.device("cuda:0")
+    tdt = torch.float32 if dtype == E.F32 else torch.float64
+    stream = torch.cuda.current_stream()
+    long_w = synth.long_object(seed=4100, n_obs=120_000, n_freq=3_000)
+    short = synth.lognormal_batch(seed=4200, n_obj=3, n_freq=3_000)
+    # objects of 120,000, then 5,000 (a slice of the long one) and three short ones
+    t = np.concatenate([long_w.t, long_w.t[:5000], short.t])
+    y = np.concatenate([long_w.y, long_w.y[:5000], short.y])
+    offs = np.concatenate([[0, 120_000, 125_000], 125_000 + short.offsets[1:]]).astype(np.uint64)
+    fmin, df, nf = long_w.fmin, long_w.df, long_w.n_freq
+    assert offs[-1] <= 131072
+    for call in range(2):
+        tt = torch.from_numpy(t).to(dev, tdt)
+        yy = torch.from_numpy(y).to(dev, tdt)
+        outs = []
+        for path in ("regular", "noalloc"):
+            pg = torch.full((offs.size - 1, nf), -1.0, dtype=tdt, device=dev)
+            bi = torch.full((offs.size - 1,), -1, dtype=torch.int32, device=dev)
+            bp = torch.full((offs.size - 1,), -1.0, dtype=tdt, device=dev)
+            if path == "regular":
+                eng.run_device(0, "mixed", tt, yy, None, offs, fmin, df, nf, True, pg, bi, bp,
+                               stream)
+            else:
+                rc = _noalloc(lib, 0, tt, yy, None, offs, fmin, df, nf, True, pg, bi, bp, stream,
+                              dtype)
+                assert rc == 0, lib.lsgb_last_error().decode()
+            torch.cuda.synchronize()
+            outs.append((pg.double().cpu().numpy(), bi.cpu().numpy(), bp.double().cpu().numpy()))
+        (pg_r, bi_r, bp_r), (pg_n, bi_n, bp_n) = outs
+        assert mixed_abs_err(pg_n, pg_r) < MIXED_ATOL, call
+        assert mixed_abs_err(bp_n, bp_r) < MIXED_ATOL
+        rows = np.arange(offs.size - 1)
+        diff = bi_n != bi_r
+        assert np.all(np.abs(pg_r[rows, bi_r] - pg_r[rows, bi_n])[diff] <= MIXED_ATOL)
+        y = y[::-1].copy()  # the second call sees different data in the same scratch
     eng.close()
 
 
