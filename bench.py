@@ -47,8 +47,13 @@ sys.path.insert(0, str(ROOT))
 METRIC = "obs x freq pairs/s (mixed form, 1 GB300)"
 UNIT = "pairs/s"
 # tensor form, standard variant: two complex products (v e^ia x e^imb, e^2ia x e^2imb),
-# each 4 real MACs x 3 split-FP16 products = 24 MACs = 48 flops per (obs, freq) pair
+# each 4 real MACs x 3 split-FP16 products = 24 MACs = 48 flops per (obs, freq) pair; the
+# algorithm itself needs 16 of them (the x3 buys FP32 accuracy from FP16 operands).
+# Generalized: three complex products (two weight groups at phase 0), 72 and 24 flops.
 TENSOR_FLOPS_PER_PAIR_STD = 48
+TENSOR_FLOPS_PER_PAIR_GEN = 72
+ALGORITHMIC_FLOPS_PER_PAIR_STD = 16
+ALGORITHMIC_FLOPS_PER_PAIR_GEN = 24
 # CUDA-core form 2 (F = 12): per observation and thread 4 (odd-lane offset) + 8 (rotation
 # to the second pair) + 4 x 4 (second-order steps) + 6 x 8 (accumulations) = 76 FP32-pipe
 # lane-ops for 12 pairs
@@ -171,6 +176,56 @@ def cpu_baseline(w, n_freq_sample: int):
                       f"({ws.pairs:.3g} pairs, {dt:.2f} s)"}
 
 
+def measure_config(eng, torch, dev, stream, flush, w, variant, err_freqs):
+    """One more benchmark workload through the default mixed form: kernel time (median of
+    runs after a first one), pairs/s, the tensor-pipe roofline, and its largest absolute
+    difference from the plain FP64 form (the drop-in arithmetic, itself pinned to the FP64
+    oracle by the tests) on the first err_freqs frequencies, with the best frequencies of
+    both forms compared there."""
+    t = torch.from_numpy(w.t).to(dev)
+    y = torch.from_numpy(w.y).to(dev)
+    dy = torch.from_numpy(w.dy).to(dev) if variant else None
+    bi = torch.empty(w.n_obj, dtype=torch.int32, device=dev)
+    bp = torch.empty(w.n_obj, dtype=torch.float64, device=dev)
+    ms = []
+    for _ in range(3):
+        flush.zero_()
+        eng.run_device(variant, "mixed", t, y, dy, w.offsets, w.fmin, w.df, w.n_freq,
+                       variant == 0, None, bi, bp, stream)
+        ms.append(eng.last_kernel_ms())
+    kms = float(np.median(ms[1:]))
+    peak_tf, peak_src = tensor_peak_tflops()
+    fpp = TENSOR_FLOPS_PER_PAIR_GEN if variant else TENSOR_FLOPS_PER_PAIR_STD
+    afpp = ALGORITHMIC_FLOPS_PER_PAIR_GEN if variant else ALGORITHMIC_FLOPS_PER_PAIR_STD
+    achieved = w.pairs * fpp / (kms / 1e3) / 1e12
+    ws = w.subset_freqs(min(err_freqs, w.n_freq))
+    pgs = {}
+    for form in ("mixed", "plain"):
+        pg = torch.empty((ws.n_obj, ws.n_freq), dtype=torch.float64, device=dev)
+        eng.run_device(variant, form, t, y, dy, ws.offsets, ws.fmin, ws.df, ws.n_freq,
+                       variant == 0, pg, None, None, stream)
+        pgs[form] = pg
+    torch.cuda.synchronize()
+    diff = float((pgs["mixed"] - pgs["plain"]).abs().max().item())
+    km = pgs["mixed"].argmax(dim=1)
+    kp = pgs["plain"].argmax(dim=1)
+    rows = torch.arange(ws.n_obj, device=dev)
+    gap = (pgs["plain"][rows, kp] - pgs["plain"][rows, km]).cpu().numpy()
+    same = int((km == kp).sum().item())
+    ties = int(((km != kp).cpu().numpy() & (gap <= 1e-4)).sum())
+    del pgs
+    return {"value": w.pairs / (kms / 1e3), "unit": UNIT, "kernel_ms": kms,
+            "pairs": w.pairs, "n_obj": w.n_obj, "rows": w.n_rows, "n_freq": w.n_freq,
+            "variant": "generalized" if variant else "standard",
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak_tf,
+                         "unit": "TFLOP/s", "frac": achieved / peak_tf, "peak_source": peak_src,
+                         "flops_per_pair": fpp, "algorithmic_flops_per_pair": afpp},
+            "max_abs_err_vs_plain_fp64": diff,
+            "error_sample": f"first {ws.n_freq} frequencies, all {ws.n_obj} objects",
+            "best_identical": same, "best_within_1e-4_tie": ties,
+            "best_other": ws.n_obj - same - ties}
+
+
 def reference_arm(args):
     """The reference's CPU path on this host (all cores), bounded sample per step."""
     from gpu_lomb_scargle_gb300 import synth
@@ -257,6 +312,9 @@ def main():
     ap.add_argument("--no-dropin", action="store_true")
     ap.add_argument("--serve-objects", type=int, default=100_000,
                     help="objects of the Poisson serving replay (0 = skip)")
+    ap.add_argument("--configs", type=int, default=1,
+                    help="also measure the single-object, generalized and long-object "
+                         "workloads (0 = skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -329,6 +387,9 @@ def main():
         roofline = {"bound": "tensor", "achieved": achieved, "peak": peak_tf, "unit": "TFLOP/s",
                     "frac": achieved / peak_tf, "traffic": TENSOR_DRAM_BYTES_PER_LAUNCH,
                     "peak_source": peak_src, "flops_per_pair": TENSOR_FLOPS_PER_PAIR_STD,
+                    "algorithmic_flops_per_pair": ALGORITHMIC_FLOPS_PER_PAIR_STD,
+                    "algorithmic_frac": achieved / peak_tf * ALGORITHMIC_FLOPS_PER_PAIR_STD
+                    / TENSOR_FLOPS_PER_PAIR_STD,
                     "kernel_ms": kms, "kernel": "tensor_kernel<standard> (lsgb_tensor.cu)"}
         # the CUDA-core form on the same batch, against the FP32 FMA peak
         saved = eng.get_tuning(0)
@@ -357,6 +418,32 @@ def main():
                     "unit": "Tops/s (FP32 pipe ops)", "frac": achieved / peak_ops, "traffic": None,
                     "peak_source": "cuBLAS SGEMM 8192^3, TF32 off, measured in this run",
                     "ops_per_pair": OPS_PER_PAIR_CUDA_CORE, "kernel_ms": kms}
+
+    # the three best frequencies per object in the same kernel pass (source/main.cu:1165-1219)
+    if tensor_form:
+        ti = torch.empty((w.n_obj, 3), dtype=torch.int32, device=dev)
+        tp = torch.empty((w.n_obj, 3), dtype=torch.float64, device=dev)
+        tm = []
+        for _ in range(3):
+            flush.zero_()
+            eng.run_device_top3(0, "mixed", t, y, None, w.offsets, w.fmin, w.df, w.n_freq, True,
+                                None, ti, tp, stream)
+            tm.append(eng.last_kernel_ms())
+        top3_ms = float(np.median(tm[1:]))
+        extra["top3"] = {"kernel_ms": top3_ms, "over_argmax": top3_ms / kms,
+                         "first_equals_argmax": bool(np.array_equal(
+                             ti[:, 0].cpu().numpy(), best_idx.astype(np.int32)))}
+
+    # the other benchmark workloads (single object, generalized batch, long object)
+    if tensor_form and args.configs:
+        extra["configs"] = {
+            "single_3555obs_1e5freq_standard": measure_config(
+                eng, torch, dev, stream, flush, synth.single_object(), 0, 100_000),
+            "lognormal_999obj_1e6freq_generalized": measure_config(
+                eng, torch, dev, stream, flush, synth.lognormal_batch_dmag(), 1, 3_000),
+            "long_200kobs_1e7freq_standard": measure_config(
+                eng, torch, dev, stream, flush, synth.long_object(), 0, 20_000),
+        }
 
     # plain FP64 drop-in form on the first plain_freqs frequencies
     if args.plain_freqs:
@@ -444,6 +531,13 @@ def main():
         extra["serving"] = rep
         extra["p50_latency_ms"] = rep["latency_p50_ms"]
         extra["p99_latency_ms"] = rep["latency_p99_ms"]
+        # a loaded point: arrivals faster than single batches are served, 1e5 frequencies
+        st2 = synth.stream(seed=5100, n_obj=max(2000, args.serve_objects // 5), rate_hz=60_000.0,
+                           n_freq=100_000)
+        rep2, _ = serve.replay(st2, slots=3, max_batch=4096, hbm_budget_bytes=4 << 30)
+        rep2["workload"] = (f"{st2.size.size} objects, Poisson 60000 objects/s, sizes "
+                            "round(LogNormal(ln 80, 0.8)) in [10, 1000], 1e5 frequencies")
+        extra["serving_loaded"] = rep2
 
     cpu = cpu_baseline(w, args.cpu_freqs) if args.cpu_freqs else None
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -23,7 +23,7 @@ LSGB_SYMBOLS = ("lsgb_engine_create", "lsgb_engine_destroy", "lsgb_last_error", 
                 "lsgb_server_submit", "lsgb_server_poll", "lsgb_server_stats", "lsgb_server_now",
                 "lsgb_server_destroy", "lsgb_set_reanchor", "lsgb_fp64_sincos_check", "lsgb_plan_create",
                 "lsgb_plan_launch", "lsgb_plan_info", "lsgb_plan_destroy", "lsgb_plan_status_async",
-                "lsgb_status_async", "lsgb_set_wait_limit")
+                "lsgb_status_async", "lsgb_set_wait_limit", "lsgb_server_peaks")
 PYABI_SYMBOLS = ("LombScarglePy", "LombScarglePy_last_status")
 
 
@@ -94,6 +94,8 @@ def lsgb() -> ctypes.CDLL:
         lib.lsgb_server_stats.argtypes = [vp, u64p]
         lib.lsgb_server_stats.restype = i32
         lib.lsgb_server_now.restype = dbl
+        lib.lsgb_server_peaks.argtypes = [vp, u64p]
+        lib.lsgb_server_peaks.restype = i32
         lib.lsgb_server_destroy.argtypes = [vp]
         lib.lsgb_server_destroy.restype = None
         lib.lsgb_set_reanchor.argtypes = [vp, u32]

@@ -123,6 +123,8 @@ struct lsgb_server {
     std::thread worker;
     std::string error;
     uint64_t batches = 0, objects_done = 0, max_batch_seen = 0;
+    uint64_t peak_busy_slots = 0, peak_waiting = 0;  // lsgb_server_peaks
+    uint64_t budget_deferrals = 0;  // admissions that stopped at the HBM budget
 };
 
 namespace {
@@ -226,14 +228,17 @@ void dispatcher(lsgb_server *s) {
         if (free_slot && !s->stop) {
             std::unique_lock<std::mutex> lk(s->mu);
             size_t rows = 0, take = 0;
+            bool over_budget = false;
             while (take < s->pending.size() && take < s->max_batch) {
                 const size_t r2 = rows + s->pending[take].t.size();
                 const size_t fp = batch_footprint(s, r2, take + 1);
-                if (s->inflight_bytes + fp > s->budget && take > 0) break;
-                if (s->inflight_bytes + fp > s->budget && s->inflight_bytes > 0) break;
+                over_budget = s->inflight_bytes + fp > s->budget &&
+                              (take > 0 || s->inflight_bytes > 0);
+                if (over_budget) break;
                 rows = r2;
                 ++take;
             }
+            if (over_budget) s->budget_deferrals++;  // objects left waiting for memory
             if (take > 0) {
                 Slot &sl = *free_slot;
                 sl.objs.assign(std::make_move_iterator(s->pending.begin()),
@@ -245,6 +250,9 @@ void dispatcher(lsgb_server *s) {
                 sl.busy = true;
                 s->batches++;
                 s->max_batch_seen = std::max<uint64_t>(s->max_batch_seen, take);
+                uint64_t busy = 0;
+                for (auto &sp : s->slots) busy += sp->busy ? 1 : 0;
+                s->peak_busy_slots = std::max(s->peak_busy_slots, busy);
                 lk.unlock();
                 const std::string err = launch(s, sl);
                 if (!err.empty()) {
@@ -339,6 +347,7 @@ LSGB_API int lsgb_server_submit(lsgb_server *s, uint64_t id, const double *t, co
         }
         p.t_submit = now_s();
         s->pending.push_back(std::move(p));
+        s->peak_waiting = std::max<uint64_t>(s->peak_waiting, s->pending.size());
     }
     s->cv.notify_one();
     return LSGB_OK;
@@ -377,6 +386,18 @@ LSGB_API int lsgb_server_stats(lsgb_server *s, uint64_t *out5) {
     out5[2] = s->max_batch_seen;
     out5[3] = s->pending.size();
     out5[4] = s->peak_inflight_bytes;
+    return LSGB_OK;
+}
+
+// Peaks: [device bytes in flight, batches (slots) in flight at once, objects waiting for
+// admission, admissions stopped at the HBM budget].
+LSGB_API int lsgb_server_peaks(lsgb_server *s, uint64_t *out4) {
+    if (!s || !out4) return LSGB_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    out4[0] = s->peak_inflight_bytes;
+    out4[1] = s->peak_busy_slots;
+    out4[2] = s->peak_waiting;
+    out4[3] = s->budget_deferrals;
     return LSGB_OK;
 }
 

@@ -30,23 +30,21 @@
 // sum with round-to-nearest adds and free at once; after the last pass of a unit they
 // compute the powers from the two running sums and free their slots (SlotRing).
 //
-// One persistent CTA per SM, warp-specialized (16 warps; warp w runs on SM sub-partition
-// w % 4):
-//   warps 0-3   fold and epilogue, one warp per TMEM lane quarter (warp w accesses lanes
-//               32 w ..): power per frequency, periodogram store, per-object maximum;
+// One persistent CTA per SM, warp-specialized:
+//   warps 0-3   fold and epilogue, one warp per TMEM lane quarter (warp w may access lanes
+//               32 (w % 4) ..): power per frequency, periodogram store, per-object maximum;
 //   warp 4      TMEM allocation and the MMA issuer (the whole warp runs the loop, one
 //               elected lane issues);
-//   warp 8      operand loader (one thread): bulk copies of a stage's A matrices from the
+//   warp 5      operand loader (one thread): bulk copies of a stage's A matrices from the
 //               operand table, and L2 prefetches of the table ahead;
-//   warps 5-7, 9-11, 13, 14
-//               producers: the split FP16 Z matrices of a stage's K-blocks, K-major without
+//   warps 6-13  producers: the split FP16 Z matrices of a stage's K-blocks, K-major without
 //               swizzle, one sine/cosine per entry, from the K-blocks' frequency steps (read
-//               from global memory one K-block ahead); the first four build a stage's first
-//               K-block, the others its second. They start as soon as the stage is free, in
-//               parallel with its bulk copy;
-//   warps 12, 15 idle (they keep sub-partition 0, which issues the MMAs, free of producers).
-// All hand-offs use mbarriers. Every wait is bounded: on a timeout the kernel records an
-// error in MixedArgs::status, lets its issued MMAs drain, frees its TMEM and returns.
+//               from global memory one stage ahead); warps 6-9 build a stage's first K-block,
+//               warps 10-13 its second. They start as soon as the stage is free, in parallel
+//               with its bulk copy.
+// All hand-offs use mbarriers. Every wait is bounded (MixedArgs::wait_cycles, by default
+// about 2 s): on a timeout the kernel records kStatusTimeout in MixedArgs::status, lets its
+// issued MMAs drain and its bulk copies land, frees its TMEM and returns.
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -61,31 +59,25 @@ namespace {
 constexpr int kTP = 128;        // fine frequency offsets p: A rows, TMEM lanes
 constexpr int kTK = 16;         // observations per K-block (the FP16 MMA depth)
 constexpr int kPassKB = 8;      // K-blocks accumulated in TMEM before an FP32 fold
-// 16 warps, four per SM sub-partition (warp w runs on sub-partition w % 4), so up to 128
-// registers per thread. The tensor pipe idles whenever the MMA warp falls behind, so the MMA
-// warp shares sub-partition 0 only with the loader, epilogue warp 0 and an idle warp; the 8
-// producer warps fill sub-partitions 1-3:
-//   sub-partition 0: epilogue 0, MMA 4, loader 8, idle 12
-//   sub-partition 1: epilogue 1, producers 5, 9, 13
-//   sub-partition 2: epilogue 2, producers 6, 10, 14
-//   sub-partition 3: epilogue 3, producers 7, 11, idle 15
-constexpr int kMmaWarp = 4;
-constexpr int kLoaderWarp = 8;
-constexpr int kProducerWarps = 8;
-constexpr int kThreads = 512;
-constexpr int kEpilogueThreads = 128;
-// Producer index 0..7 of warps 5, 6, 7, 9, 10, 11, 13, 14; -1 for the other warps.
-__device__ __forceinline__ int producer_index(int warp) {
-    if (warp < 5 || warp > 14 || (warp & 3) == 0) return -1;
-    return warp - 4 - (warp >> 2);
-}
+constexpr int kLoaderWarp = 5;
+constexpr int kProducerWarp0 = 6;
+// 14 warps in all, at most 4 per SM sub-partition, so up to 128 registers per thread:
+// kEpiPerQuarter epilogue warps per TMEM lane quarter. 1: warps 0-3 and 8 producer warps;
+// 2: warps 0-3 and the four after 4 producer warps (the producers then fall behind the
+// MMA warp: 2-3% slower)
+constexpr int kEpiPerQuarter = 1;
+constexpr int kProducerWarps = kEpiPerQuarter == 2 ? 4 : 8;
+constexpr int kEpilogueWarp1 = kProducerWarp0 + kProducerWarps;  // second epilogue group
+constexpr int kThreads = 32 * (kEpilogueWarp1 + (kEpiPerQuarter == 2 ? 4 : 0));
+constexpr int kEpilogueThreads = 128 * kEpiPerQuarter;
 constexpr uint32_t kPrefetchKB = 32;   // operand-table K-blocks prefetched into L2 ahead
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kSlots = 4;       // TMEM accumulator slots
 constexpr uint32_t kSlotCols = 128;  // TMEM columns of one slot
 // Default limit of a bounded wait (MixedArgs::wait_cycles overrides it for the pipeline
-// waits); the final waits for the CTA's own copies and MMAs in flight always use it.
+// waits); the final waits for the CTA's own MMAs in flight always use it.
 constexpr long long kWaitCycles = 1ll << 32;  // ~2 s at 2 GHz
+constexpr long long kAbortCopyCycles = 1ll << 21;  // ~1 ms: in-flight copies after an abort
 
 // Per-variant geometry.
 template <bool GEN>
@@ -101,13 +93,9 @@ struct TGeo {
     static constexpr int A_BYTES = kTP * kTK * 2;  // one 128 x 16 FP16 matrix
     static constexpr int Z_ROWS = 3 * G0 * NM;     // [-Bi; Br; Bi], each G rows blocks of NM
     static constexpr int Z_BYTES = Z_ROWS * kTK * 2;
-    // stage: KPS consecutive K-blocks of one phase: their A matrices (re/im, hi/lo; AKB
-    // bytes each), then their Z matrices (hi, lo; ZKB bytes each). The MMA warp waits once
-    // and commits at most once per stage of 6 KPS = 12 MMAs (each tcgen05.commit costs the
-    // tensor pipe about 250 cycles at N = 128), and the last stage of a pass is released by
-    // the pass's own accumulator commit. Four stages of 56 KB fill the shared memory (two
-    // stages of four K-blocks, one commit per 24 MMAs, left too little time to refill a
-    // stage and were 4% slower).
+    // stage: KPS consecutive K-blocks of one phase, so that the MMA warp waits and
+    // commits once per 6 KPS MMAs: their A matrices (re/im, hi/lo; AKB bytes each), then
+    // their Z matrices (hi, lo; ZKB bytes each)
     static constexpr int KPS = 2;
     static constexpr int AKB = 4 * A_BYTES;
     static constexpr int ZKB = 2 * Z_BYTES;
@@ -123,7 +111,7 @@ struct TGeo {
     static constexpr int SB = GEN ? 16 : 8;
     static_assert(W0 <= (int)kSlotCols && W1 <= (int)kSlotCols, "TMEM slot too narrow");
     static_assert(kSlots * kSlotCols == kTmemCols, "TMEM layout");
-    static_assert(NM % 32 == 0 && KPS % 2 == 0, "producer mapping: two groups");
+    static_assert(NM % 32 == 0 && kProducerWarps % KPS == 0, "producer mapping");
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -201,16 +189,32 @@ __device__ __forceinline__ bool mbar_test(uint64_t *b, uint32_t parity) {
     return done != 0;
 }
 
+// Non-blocking test of the phase of `parity` of barrier b.
+__device__ __forceinline__ bool mbar_test_now(uint64_t *b, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2; "
+        "selp.u32 %0, 1, 0, p; }"
+        : "=r"(done)
+        : "r"(smem_u32(b)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
 // Waits for the phase of `parity` of barrier b for at most `limit` cycles. Returns false
 // (and raises the CTA's abort flag and the launch's status) on a timeout or when another
-// role aborted.
+// role aborted. With the default limit it polls with try_wait (which may suspend the thread
+// until the phase completes) and looks at the clock and the abort flag every 256 polls; a
+// shorter limit (lsgb_set_wait_limit, for tests) polls without suspending and looks every
+// time, so that it is kept to the cycle.
 __device__ __noinline__ bool mbar_wait_slow(uint64_t *b, uint32_t parity,
                                             volatile uint32_t *abort, uint32_t *status,
                                             long long limit) {
     const long long t0 = clock64();
+    const bool exact = limit < kWaitCycles;
     for (uint32_t it = 1;; ++it) {
-        if (mbar_test(b, parity)) return true;
-        if ((it & 255u) == 0) {
+        if (exact ? mbar_test_now(b, parity) : mbar_test(b, parity)) return true;
+        if (exact || (it & 255u) == 0) {
             if (*abort) return false;
             if (clock64() - t0 > limit) {
                 *abort = 1u;
@@ -220,10 +224,12 @@ __device__ __noinline__ bool mbar_wait_slow(uint64_t *b, uint32_t parity,
         }
     }
 }
-// The completed case inline, the polling loop out of line.
+// The completed case inline (one try_wait), the polling loop out of line; a shorter limit
+// goes straight to the loop's non-blocking polls.
 __device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, volatile uint32_t *abort,
                                           uint32_t *status, long long limit) {
-    return mbar_test(b, parity) || mbar_wait_slow(b, parity, abort, status, limit);
+    return (limit >= kWaitCycles && mbar_test(b, parity)) ||
+           mbar_wait_slow(b, parity, abort, status, limit);
 }
 
 __device__ __forceinline__ void bulk_prefetch_l2(const void *src, uint32_t bytes) {
@@ -383,102 +389,26 @@ struct UnitWalk {
 // Which TMEM slot each pass accumulates into. Free slots are handed out in the order they
 // were freed: pop() for every pass in order; a phase's first pass keeps its slot as the
 // running sum, a later pass's slot is pushed back once the epilogue has folded it, and the
-// unit's two running-sum slots are pushed back after its power pass. The MMA warp, the
-// epilogue warps and the fill side (StageRelease) run this same bookkeeping over the same
-// sequence of passes, so they agree on every pass's slot without exchanging it. At most
-// two slots are held across a pass boundary (the running sums), so a pop always finds one,
-// and a slot is used again at least two passes after its previous use. pop() also gives
-// the slot's use count (mod 4): use u is released to the epilogue by a commit on
-// sfull_bar[2 slot + (u & 1)], phase u >> 1 (two alternating barriers per slot, see
-// StageRelease), and handed back by the epilogue on sempty_bar[slot], phase u.
+// unit's two running-sum slots are pushed back after its power pass. The MMA warp and the
+// epilogue warps run this same bookkeeping over the same sequence of passes, so they agree
+// on every pass's slot without exchanging it. At most two slots are held across a pass
+// boundary (the running sums), so a pop always finds one; the slot's barriers alternate
+// between its full and empty phases, whose parity is the count of its uses so far.
 struct SlotRing {
     uint32_t q = 0xE4u;  // queued free slots, 2 bits each, head in the low bits: 0, 1, 2, 3
     uint32_t n = kSlots;
-    uint32_t uses = 0u;  // bits 2s, 2s + 1: uses of slot s so far, mod 4
-    __device__ __forceinline__ uint32_t pop(uint32_t &use) {
+    uint32_t par = 0u;   // bit s: parity of slot s's uses before the current one
+    __device__ __forceinline__ uint32_t pop(uint32_t &parity) {
         const uint32_t s = q & 3u;
         q >>= 2;
         --n;
-        use = (uses >> (2u * s)) & 3u;
-        uses = (uses & ~(3u << (2u * s))) | (((use + 1u) & 3u) << (2u * s));
+        parity = (par >> s) & 1u;
+        par ^= 1u << s;
         return s;
     }
     __device__ __forceinline__ void push(uint32_t s) {
         q |= s << (2u * n);
         ++n;
-    }
-};
-// The barrier and parity that signal the completion of use `use` of a slot.
-__device__ __forceinline__ uint32_t sfull_index(uint32_t slot, uint32_t use) {
-    return 2u * slot + (use & 1u);
-}
-__device__ __forceinline__ uint32_t sfull_parity(uint32_t use) { return (use >> 1) & 1u; }
-
-// The fill side's view of the stage ring (the loader and the producers). A stage is free
-// again once the MMAs that read it have completed. The MMA warp signals that with a commit
-// on empty_bar[s] after a stage that is not the last of its pass; the last stage of a pass
-// is released by the pass's accumulator commit (the one that also hands the TMEM slot to the
-// epilogue), which saves one of the pass's commits. The fill side replays the MMA warp's
-// slot bookkeeping over the same pass sequence, so it knows each pass's slot and use, and
-// records how the latest use of each stage slot is released; before it fills the stage slot
-// again it waits for that release.
-//
-// No such wait can see its barrier two phases ahead, which would make the parity test
-// ambiguous: the next commit on the same empty barrier comes after a later stage in the same
-// stage slot, and the next completion on the same sfull barrier is two uses of the slot
-// later, at least four passes (four stages) on; both need the stage this wait is for.
-template <int S>
-struct StageRelease {
-    SlotRing ring;
-    uint32_t slot = 0, use = 0;   // the current pass's TMEM slot and its use count
-    uint32_t rsum[2] = {0u, 0u};  // the unit's running-sum slots
-    uint32_t rel[S] = {};         // release of stage slot s's latest use: bit 31 set:
-                                  // sfull_bar[rel & 7], parity bit 3; else empty_bar[s],
-                                  // parity bit 0 (read and written with constant indices,
-                                  // so that it stays in registers)
-    uint32_t epar = 0u;           // bit s: parity of the next commit on empty_bar[s]
-    uint32_t g = 0u;              // stages filled so far
-    // Begins the stage whose first K-block is sb; returns its stage slot.
-    __device__ __forceinline__ uint32_t begin(uint32_t sb) {
-        if (sb % kPassKB == 0) slot = ring.pop(use);
-        return g % S;
-    }
-    // Waits until the stage slot's previous use is released (always true for the first S).
-    __device__ __forceinline__ bool wait_free(uint64_t *empty_bar, uint64_t *sfull_bar,
-                                              volatile uint32_t *abort, uint32_t *status,
-                                              long long lim) const {
-        if (g < (uint32_t)S) return true;
-        const uint32_t s = g % S;
-        uint32_t r = rel[0];
-#pragma unroll
-        for (int i = 1; i < S; ++i)
-            if (s == (uint32_t)i) r = rel[i];
-        return (r >> 31) ? mbar_wait(&sfull_bar[r & 7u], (r >> 3) & 1u, abort, status, lim)
-                         : mbar_wait(&empty_bar[s], r & 1u, abort, status, lim);
-    }
-    // Ends the stage: records how it is released, replays the pass-end bookkeeping.
-    template <int KPS>
-    __device__ __forceinline__ void end(uint32_t sb, uint32_t nkb, uint32_t ph) {
-        const uint32_t s = g % S;
-        const uint32_t pend = min(nkb, (sb / kPassKB) * kPassKB + kPassKB);
-        uint32_t r;
-        if (sb + (uint32_t)KPS >= pend) {  // last stage of its pass
-            r = 0x80000000u | sfull_index(slot, use) | (sfull_parity(use) << 3);
-            if (sb >= (uint32_t)kPassKB) ring.push(slot);
-            else if (ph) rsum[1] = slot;  // constant indices keep rsum in registers
-            else rsum[0] = slot;
-        } else {
-            r = (epar >> s) & 1u;
-            epar ^= 1u << s;
-        }
-#pragma unroll
-        for (int i = 0; i < S; ++i)
-            if (s == (uint32_t)i) rel[i] = r;
-        ++g;
-    }
-    __device__ __forceinline__ void unit_end() {
-        ring.push(rsum[0]);
-        ring.push(rsum[1]);
     }
 };
 
@@ -489,17 +419,13 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *ring = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    // copy: the stage's A matrices have landed (the loader's arrival and the bulk copy's
-    // bytes); full: the stage is ready for the MMAs, i.e. its Z matrices are written (one
-    // arrival per producer warp) and, since the first producer warp arrives only after it
-    // has seen the copy, its A matrices too; empty: its MMAs have completed (the loader and
-    // the producers wait for it). The copy has a barrier of its own so that the loader can
-    // always wait for its copies to land before the CTA exits, also when another role has
-    // aborted and the stage never becomes full.
-    __shared__ __align__(8) uint64_t copy_bar[S], full_bar[S], empty_bar[S];
+    // full: the stage's A matrices have landed (the loader's arrival and bytes) and its Z
+    // matrix is written (the producers' arrivals); empty: its MMAs have completed (the
+    // loader and the producers wait for it)
+    __shared__ __align__(8) uint64_t full_bar[S], empty_bar[S];
     // sfull: a pass's MMAs into the slot have completed; sempty: the epilogue has folded the
     // slot or, for a running sum, finished the unit's power pass
-    __shared__ __align__(8) uint64_t sfull_bar[2 * kSlots], sempty_bar[kSlots], drain_bar;
+    __shared__ __align__(8) uint64_t sfull_bar[kSlots], sempty_bar[kSlots], drain_bar;
     __shared__ uint32_t s_tmem;
     __shared__ volatile uint32_t s_abort;
 
@@ -509,19 +435,18 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
 
     if (tid == 0) {
         for (int s = 0; s < S; ++s) {
-            mbar_init(&copy_bar[s], 1);
-            mbar_init(&full_bar[s], kProducerWarps);  // one arrival per producer warp
+            mbar_init(&full_bar[s], kProducerWarps + 1);  // one arrival per producer warp
             mbar_init(&empty_bar[s], 1);
         }
-        for (uint32_t b = 0; b < 2 * kSlots; ++b) mbar_init(&sfull_bar[b], 1);
         for (uint32_t b = 0; b < kSlots; ++b) {
+            mbar_init(&sfull_bar[b], 1);
             mbar_init(&sempty_bar[b], kEpilogueThreads / 32);  // one arrival per warp
         }
         mbar_init(&drain_bar, 1);
         s_abort = 0u;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == kMmaWarp) {
+    if (warp == 4) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          smem_u32(&s_tmem)),
                      "r"(kTmemCols)
@@ -536,20 +461,18 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
     // Every role walks the same sequence: units b, b + grid, ...; in each unit phase 0
     // (exp(i theta) sums) then phase 1 (exp(2i theta) sums), each over the unit's nkb
     // K-blocks, cut into passes of kPassKB K-blocks.
-    if (producer_index(warp) >= 0) {
+    if (warp >= kProducerWarp0 && warp < kEpilogueWarp1) {
         // ---------------- producers ----------------
         // Z entry (m, j): B = exp(i (kT + 128 m) b_j) (phase 0) or its square (phase 1).
-        // The producer warps come in two groups of four, group hk building the KPW K-blocks
-        // KPW hk .. KPW hk + KPW - 1 of every stage. A thread owns row m and the JPT
-        // observations j0.. of its K-block: one 2 JPT-byte store per row kind (-Bi, Br, Bi)
-        // and half (hi, lo). The lanes of a quarter-warp own 8 consecutive rows of one core
-        // matrix, so the stores have no bank conflicts.
-        constexpr uint32_t KPW = (uint32_t)G::KPS / 2u;  // K-blocks a group builds per stage
-        constexpr uint32_t GW = (uint32_t)kProducerWarps / 2u;  // warps a group
+        // The producer warps come in KPS groups, group hk building K-block hk of every stage.
+        // A thread owns row m and the JPT observations j0.. of its K-block: one 2 JPT-byte
+        // store per row kind (-Bi, Br, Bi) and half (hi, lo). The lanes of a quarter-warp
+        // own 8 consecutive rows of one core matrix, so the stores have no bank conflicts.
+        constexpr uint32_t GW = (uint32_t)kProducerWarps / (uint32_t)G::KPS;  // warps a group
         constexpr uint32_t JPT = (uint32_t)G::NM * kTK / (32u * GW);
         constexpr uint32_t JS = kTK / JPT;
         static_assert(JPT == 4 || JPT == 8, "producer mapping");
-        const uint32_t pw = (uint32_t)producer_index(warp);
+        const uint32_t pw = (uint32_t)(warp - kProducerWarp0);
         const uint32_t hk = pw / GW;
         // quarter-warp c of the group: observation slice c % JS, row group c / JS
         const uint32_t c = ((uint32_t)lane >> 3) + 4u * (pw % GW);
@@ -557,13 +480,13 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
         const uint32_t j0 = JPT * (c % JS);
         // group g of G: rows g NM + m (-Bi), (G + g) NM + m (Br), (2G + g) NM + m (Bi) of the
         // hi matrix; lo is Z_BYTES further
-        const uint32_t zo = (uint32_t)G::Z_OFF + kmaj_off(m, j0);
+        const uint32_t zo = (uint32_t)G::Z_OFF + hk * (uint32_t)G::ZKB + kmaj_off(m, j0);
         constexpr uint32_t kRowNM = (uint32_t)G::NM * 32u;  // kmaj_off(r + NM) - kmaj_off(r)
-        StageRelease<S> rs;
+        uint32_t g = 0;
         UnitWalk walk(a, units);
-        // the steps (and weights) of the next K-block this thread builds, loaded one K-block
+        // the steps (and weights) of the group's K-block of the next stage, loaded one stage
         // ahead (only for K-blocks that exist)
-        constexpr uint32_t NQ4 = JPT * (uint32_t)G::SB / 16u;  // uint4 per thread and K-block
+        constexpr uint32_t NQ4 = JPT * (uint32_t)G::SB / 16u;  // uint4 per thread and stage
         const uint4 *steps = static_cast<const uint4 *>(a.steps);
         uint4 nb[NQ4];
         auto load_b = [&](uint32_t kbg) {
@@ -571,7 +494,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             for (uint32_t h = 0; h < NQ4; ++h)
                 nb[h] = __ldg(steps + (kbg * kTK + j0) * (uint32_t)G::SB / 16u + h);
         };
-        if (blockIdx.x < units && KPW * hk < walk.nxt.nkb) load_b(walk.nxt.kb0 + KPW * hk);
+        if (blockIdx.x < units && hk < walk.nxt.nkb) load_b(walk.nxt.kb0 + hk);
         // the warp's lanes leave together: the abort flag as lane 0 reads it, and every
         // wait's outcome voted over the warp
         for (uint32_t u = blockIdx.x; u < units && __shfl_sync(0xffffffffu, s_abort, 0) == 0u;
@@ -582,98 +505,92 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             bool ok = true;
             for (uint32_t st = 0; st < 2u * nsp; ++st) {
                 const bool ph1 = st >= nsp;
-                const uint32_t sb = (ph1 ? st - nsp : st) * (uint32_t)G::KPS;  // first K-block
-                const uint32_t s = rs.begin(sb);
+                const uint32_t kb = (ph1 ? st - nsp : st) * (uint32_t)G::KPS + hk;
+                const bool mine = kb < w.nkb;
+                uint4 cb[NQ4];
+#pragma unroll
+                for (uint32_t h = 0; h < NQ4; ++h) cb[h] = nb[h];
+                // the group's K-block of the next stage: this unit's, or the next unit's first
+                {
+                    const uint32_t st1 = st + 1u;
+                    if (st1 < 2u * nsp) {
+                        const uint32_t kb1 = (st1 >= nsp ? st1 - nsp : st1) * (uint32_t)G::KPS + hk;
+                        if (kb1 < w.nkb) load_b(w.kb0 + kb1);
+                    } else if (u + gridDim.x < units && hk < walk.nxt.nkb) {
+                        load_b(walk.nxt.kb0 + hk);
+                    }
+                }
+                const uint32_t s = g % S, us = g / S;
                 if (!__all_sync(0xffffffffu,
-                                rs.wait_free(empty_bar, sfull_bar, &s_abort, a.status, lim))) {
+                                mbar_wait(&empty_bar[s], (us & 1u) ^ 1u, &s_abort, a.status, lim))) {
                     ok = false;
                     break;
                 }
-#pragma unroll 1
-                for (uint32_t i = 0; i < KPW; ++i) {
-                    const uint32_t kbi = KPW * hk + i;  // K-block of the stage
-                    const uint32_t kb = sb + kbi;
-                    const bool mine = kb < w.nkb;
-                    uint4 cb[NQ4];
+                if (mine) {
+                    unsigned char *zh = ring + (size_t)s * G::STAGE + zo;
+                    auto put = [&](unsigned char *dst, const uint32_t (&v)[JPT / 2]) {
+                        if constexpr (JPT == 8)
+                            *reinterpret_cast<uint4 *>(dst) = make_uint4(v[0], v[1], v[2], v[3]);
+                        else
+                            *reinterpret_cast<uint2 *>(dst) = make_uint2(v[0], v[1]);
+                    };
+                    // the observations in pairs (j, j + 1): cos / sin of k b_j (or of twice
+                    // it), times the group weights, split and packed as FP16 pairs
+                    const uint32_t ng = (GEN && !ph1) ? 2u : 1u;
+                    uint32_t pch[2][JPT / 2], pcl[2][JPT / 2], psh[2][JPT / 2], psl[2][JPT / 2];
 #pragma unroll
-                    for (uint32_t h = 0; h < NQ4; ++h) cb[h] = nb[h];
-                    // the next K-block this thread builds: the stage's next one, the next
-                    // stage's first, or the next unit's first
-                    if (i + 1u < KPW) {
-                        if (kb + 1u < w.nkb) load_b(w.kb0 + kb + 1u);
-                    } else if (st + 1u < 2u * nsp) {
-                        const uint32_t st1 = st + 1u;
-                        const uint32_t kb1 = (st1 >= nsp ? st1 - nsp : st1) * (uint32_t)G::KPS + KPW * hk;
-                        if (kb1 < w.nkb) load_b(w.kb0 + kb1);
-                    } else if (u + gridDim.x < units && KPW * hk < walk.nxt.nkb) {
-                        load_b(walk.nxt.kb0 + KPW * hk);
+                    for (uint32_t h = 0; h < JPT / 2; ++h) {
+                        uint32_t bl[2], bh[2];
+                        float wt[2][2];  // [observation][group]
+                        if constexpr (GEN) {
+                            const uint4 q0 = cb[2 * h], q1 = cb[2 * h + 1];
+                            bl[0] = q0.x; bh[0] = q0.y; bl[1] = q1.x; bh[1] = q1.y;
+                            wt[0][0] = __uint_as_float(q0.z); wt[0][1] = __uint_as_float(q0.w);
+                            wt[1][0] = __uint_as_float(q1.z); wt[1][1] = __uint_as_float(q1.w);
+                        } else {
+                            bl[0] = cb[h].x; bh[0] = cb[h].y; bl[1] = cb[h].z; bh[1] = cb[h].w;
+                            wt[0][0] = wt[0][1] = wt[1][0] = wt[1][1] = 1.0f;
+                        }
+                        float sn[2], cs[2];
+#pragma unroll
+                        for (int q = 0; q < 2; ++q) {
+                            // hi 32 bits of k b mod 2^64: (k b_lo) >> 32 plus k b_hi
+                            const uint32_t t32 = __umulhi(k, bl[q]) + k * bh[q];
+                            // phase 1: the doubled angle is the doubled turn count (mod 2^32)
+                            turn_sincos(ph1 ? t32 << 1 : t32, sn[q], cs[q]);
+                        }
+                        // the two observations as packed pairs
+                        const uint64_t C = pack2(cs[0], cs[1]), Sn = pack2(sn[0], sn[1]);
+#pragma unroll
+                        for (int gi = 0; gi < (GEN ? 2 : 1); ++gi) {
+                            if (gi >= (int)ng) break;  // phase 1 has one group
+                            uint64_t Cg = C, Sg = Sn;
+                            if (GEN) {
+                                const uint64_t W = pack2(wt[0][gi], wt[1][gi]);
+                                Cg = fmul2(C, W);
+                                Sg = fmul2(Sn, W);
+                            }
+                            split2(Cg, pch[gi][h], pcl[gi][h]);
+                            split2(Sg, psh[gi][h], psl[gi][h]);
+                        }
                     }
-                    if (mine) {
-                        unsigned char *zh = ring + (size_t)s * G::STAGE + zo + kbi * (uint32_t)G::ZKB;
-                        auto put = [&](unsigned char *dst, const uint32_t (&v)[JPT / 2]) {
-                            if constexpr (JPT == 8)
-                                *reinterpret_cast<uint4 *>(dst) = make_uint4(v[0], v[1], v[2], v[3]);
-                            else
-                                *reinterpret_cast<uint2 *>(dst) = make_uint2(v[0], v[1]);
-                        };
-                        // the observations in pairs (j, j + 1): cos / sin of k b_j (or of twice
-                        // it), times the group weights, split and packed as FP16 pairs
-                        const uint32_t ng = (GEN && !ph1) ? 2u : 1u;
-                        uint32_t pch[2][JPT / 2], pcl[2][JPT / 2], psh[2][JPT / 2], psl[2][JPT / 2];
+#pragma unroll
+                    for (uint32_t gi = 0; gi < (GEN ? 2u : 1u); ++gi) {
+                        if (gi >= ng) break;
+                        // -x = (-hi) + (-lo) exactly: the sign bits of both FP16 halves flipped
+                        uint32_t nsh[JPT / 2], nsl[JPT / 2];
 #pragma unroll
                         for (uint32_t h = 0; h < JPT / 2; ++h) {
-                            uint32_t bl[2], bh[2];
-                            float wt[2][2];  // [observation][group]
-                            if constexpr (GEN) {
-                                const uint4 q0 = cb[2 * h], q1 = cb[2 * h + 1];
-                                bl[0] = q0.x; bh[0] = q0.y; bl[1] = q1.x; bh[1] = q1.y;
-                                wt[0][0] = __uint_as_float(q0.z); wt[0][1] = __uint_as_float(q0.w);
-                                wt[1][0] = __uint_as_float(q1.z); wt[1][1] = __uint_as_float(q1.w);
-                            } else {
-                                bl[0] = cb[h].x; bh[0] = cb[h].y; bl[1] = cb[h].z; bh[1] = cb[h].w;
-                                wt[0][0] = wt[0][1] = wt[1][0] = wt[1][1] = 1.0f;
-                            }
-                            float sn[2], cs[2];
-#pragma unroll
-                            for (int q = 0; q < 2; ++q) {
-                                // hi 32 bits of k b mod 2^64: (k b_lo) >> 32 plus k b_hi
-                                const uint32_t t32 = __umulhi(k, bl[q]) + k * bh[q];
-                                // phase 1: the doubled angle is the doubled turn count (mod 2^32)
-                                turn_sincos(ph1 ? t32 << 1 : t32, sn[q], cs[q]);
-                            }
-                            // the two observations as packed pairs
-                            const uint64_t C = pack2(cs[0], cs[1]), Sn = pack2(sn[0], sn[1]);
-#pragma unroll
-                            for (int gi = 0; gi < (GEN ? 2 : 1); ++gi) {
-                                if (gi >= (int)ng) break;  // phase 1 has one group
-                                uint64_t Cg = C, Sg = Sn;
-                                if (GEN) {
-                                    const uint64_t W = pack2(wt[0][gi], wt[1][gi]);
-                                    Cg = fmul2(C, W);
-                                    Sg = fmul2(Sn, W);
-                                }
-                                split2(Cg, pch[gi][h], pcl[gi][h]);
-                                split2(Sg, psh[gi][h], psl[gi][h]);
-                            }
+                            nsh[h] = psh[gi][h] ^ 0x80008000u;
+                            nsl[h] = psl[gi][h] ^ 0x80008000u;
                         }
-#pragma unroll
-                        for (uint32_t gi = 0; gi < (GEN ? 2u : 1u); ++gi) {
-                            if (gi >= ng) break;
-                            // -x = (-hi) + (-lo) exactly: the sign bits of both FP16 halves flipped
-                            uint32_t nsh[JPT / 2], nsl[JPT / 2];
-#pragma unroll
-                            for (uint32_t h = 0; h < JPT / 2; ++h) {
-                                nsh[h] = psh[gi][h] ^ 0x80008000u;
-                                nsl[h] = psl[gi][h] ^ 0x80008000u;
-                            }
-                            unsigned char *zg = zh + gi * kRowNM;
-                            put(zg, nsh);
-                            put(zg + G::Z_BYTES, nsl);
-                            put(zg + ng * kRowNM, pch[gi]);
-                            put(zg + ng * kRowNM + G::Z_BYTES, pcl[gi]);
-                            put(zg + 2u * ng * kRowNM, psh[gi]);
-                            put(zg + 2u * ng * kRowNM + G::Z_BYTES, psl[gi]);
-                        }
+                        unsigned char *zg = zh + gi * kRowNM;
+                        put(zg, nsh);
+                        put(zg + G::Z_BYTES, nsl);
+                        put(zg + ng * kRowNM, pch[gi]);
+                        put(zg + ng * kRowNM + G::Z_BYTES, pcl[gi]);
+                        put(zg + 2u * ng * kRowNM, psh[gi]);
+                        put(zg + 2u * ng * kRowNM + G::Z_BYTES, psl[gi]);
                     }
                 }
                 // generic-proxy stores -> the MMA's async-proxy reads; then one arrival for
@@ -681,24 +598,16 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                 // lanes have fenced
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 __syncwarp();
-                // the first producer warp arrives once the stage's bulk copy has landed, so
-                // that the full barrier also covers the A matrices (lap g / S of the stage)
-                if (pw == 0 && !__all_sync(0xffffffffu, mbar_wait(&copy_bar[s], (rs.g / S) & 1u,
-                                                                  &s_abort, a.status, lim))) {
-                    ok = false;
-                    break;
-                }
                 if (lane == 0) mbar_arrive(&full_bar[s]);
-                rs.template end<G::KPS>(sb, w.nkb, ph1 ? 1u : 0u);
+                ++g;
             }
             if (!ok) break;
-            rs.unit_end();
         }
     } else if (warp == kLoaderWarp) {
         // ---------------- operand loader ----------------
         if (lane == 0) {
             const unsigned char *tab = static_cast<const unsigned char *>(a.optab);
-            StageRelease<S> rs;
+            uint32_t g = 0;
             UnitWalk walk(a, units);
             const uint64_t tph = (uint64_t)a.total_kb * G::AKB;  // phase stride of the table
             auto prefetch = [&](uint32_t kbg, uint32_t n) {  // K-blocks kbg.. of both phases
@@ -713,40 +622,27 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                 if (u + gridDim.x < units) prefetch(walk.nxt.kb0, min(walk.nxt.nkb, kPrefetchKB));
                 bool ok = true;
                 for (uint32_t ph = 0; ph < 2u && ok; ++ph) {
-                    for (uint32_t kb = 0; kb < w.nkb; kb += G::KPS) {
-                        const uint32_t s = rs.begin(kb);
+                    for (uint32_t kb = 0; kb < w.nkb; kb += G::KPS, ++g) {
+                        const uint32_t s = g % S, us = g / S;
                         const uint32_t cnt = min((uint32_t)G::KPS, w.nkb - kb);
                         if (!ph && kb + kPrefetchKB < w.nkb)
                             prefetch(w.kb0 + kb + kPrefetchKB, min(cnt, w.nkb - kb - kPrefetchKB));
-                        if (!rs.wait_free(empty_bar, sfull_bar, &s_abort, a.status, lim)) {
+                        if (!mbar_wait(&empty_bar[s], (us & 1u) ^ 1u, &s_abort, a.status, lim)) {
                             ok = false;
                             break;
                         }
                         const uint32_t bytes = cnt * (uint32_t)G::AKB;
-                        mbar_expect_tx(&copy_bar[s], bytes);
+                        mbar_expect_tx(&full_bar[s], bytes);
                         bulk_copy_g2s(ring + (size_t)s * G::STAGE,
                                       tab + ph * tph + (uint64_t)(w.kb0 + kb) * G::AKB, bytes,
-                                      &copy_bar[s]);
-                        rs.template end<G::KPS>(kb, w.nkb, ph);
+                                      &full_bar[s]);
                     }
                 }
                 if (!ok) break;
-                rs.unit_end();
-            }
-            // Before the CTA may exit, every bulk copy it issued must have landed (after an
-            // abort some stages are never consumed): the latest copy into stage slot s is the
-            // slot's lap ceil((g - s) / S) - 1; waited for with the default limit.
-#pragma unroll
-            for (uint32_t s = 0; s < (uint32_t)S; ++s) {
-                if (rs.g <= s) continue;
-                const uint32_t laps = (rs.g - s + (uint32_t)S - 1u) / (uint32_t)S;
-                const long long t0 = clock64();
-                while (!mbar_test(&copy_bar[s], (laps - 1u) & 1u) && clock64() - t0 < kWaitCycles) {
-                }
             }
         }
         __syncwarp();
-    } else if (warp == kMmaWarp) {
+    } else if (warp == 4) {
         // ---------------- MMA issuer ----------------
         // The whole warp walks the loop (every value in it is warp-uniform and every wait
         // ends in a vote); one elected lane issues the MMAs and commits.
@@ -770,9 +666,9 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                 const UnitInfo w = walk.next(a, u, units);  // nkb >= 1: no object is empty
                 for (uint32_t ph = 0; ph < 2 && ok; ++ph) {
                     for (uint32_t kb0 = 0; kb0 < w.nkb && ok; kb0 += kPassKB) {
-                        uint32_t use;
-                        const uint32_t slot = ring.pop(use);
-                        if (!__all_sync(0xffffffffu, mbar_wait(&sempty_bar[slot], (use & 1u) ^ 1u,
+                        uint32_t sp;
+                        const uint32_t slot = ring.pop(sp);
+                        if (!__all_sync(0xffffffffu, mbar_wait(&sempty_bar[slot], sp ^ 1u,
                                                                &s_abort, a.status, lim))) {
                             ok = false;
                             break;
@@ -808,8 +704,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                                                         dsc(dlo, ao + 3 * G::A_BYTES)};
                                 mma_cplx6(d0, ad, bd, idesc, acc0);
                             }
-                            // the pass's last stage is released by the pass's commit below
-                            if (kb + (uint32_t)G::KPS < kb1) mma_commit(&empty_bar[s]);
+                            mma_commit(&empty_bar[s]);
                             if (++s == (uint32_t)S) {
                                 s = 0;
                                 sph ^= 1u;
@@ -818,7 +713,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                                 dlo += (uint32_t)G::STAGE >> 4;
                             }
                         }
-                        if (ok) mma_commit(&sfull_bar[sfull_index(slot, use)]);
+                        if (ok) mma_commit(&sfull_bar[slot]);
                         // the epilogue's side of the bookkeeping
                         if (kb0 == 0) rsum[ph] = slot;
                         else ring.push(slot);
@@ -834,13 +729,16 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             }
         }
         __syncwarp();
-    } else if (warp < 4) {
+    } else {
         // ---------------- fold and epilogue ----------------
-        // warp w (0-3) accesses TMEM lanes 32 w .. 32 w + 31: the fine offsets p of its
-        // lanes, all NM coarse steps of every quantity block
+        // warp w may access TMEM lanes 32 (w % 4) ..; with two warps per lane quarter they
+        // split the coarse steps: warp half eh owns m in [eh SPAN, (eh+1) SPAN), i.e. the same
+        // part of every NM-column quantity block, in the folds and in the power pass, so a
+        // warp only ever reads running sums it wrote itself
         const uint32_t eq = (uint32_t)warp & 3u;
-        const uint32_t eh = 0u;
-        constexpr uint32_t SPAN = (uint32_t)G::NM;  // columns of each quantity block
+        const uint32_t eh = (kEpiPerQuarter == 2 && warp >= kEpilogueWarp1) ? 1u : 0u;
+        // columns of each NM-column quantity block this warp folds and reads: SPAN from eh SPAN
+        constexpr uint32_t SPAN = (uint32_t)G::NM / (uint32_t)kEpiPerQuarter;
         const uint32_t pl = eq * 32u + (uint32_t)lane;
         const uint32_t lane_base = (eq * 32u) << 16;
         bool ok = true;
@@ -857,11 +755,9 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             for (uint32_t ph = 0; ph < 2 && ok; ++ph) {
                 const uint32_t wcols = ph ? (uint32_t)G::W1 : (uint32_t)G::W0;
                 for (uint32_t pi = 0; pi < npass; ++pi) {
-                    uint32_t use;
-                    const uint32_t slot = ring.pop(use);
-                    if (!__all_sync(0xffffffffu, mbar_wait(&sfull_bar[sfull_index(slot, use)],
-                                                           sfull_parity(use), &s_abort, a.status,
-                                                           lim))) {
+                    uint32_t sp;
+                    const uint32_t slot = ring.pop(sp);
+                    if (!__all_sync(0xffffffffu, mbar_wait(&sfull_bar[slot], sp, &s_abort, a.status, lim))) {
                         ok = false;
                         break;
                     }
@@ -1050,7 +946,18 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
 
     tc_fence_before();
     __syncthreads();
-    if (warp == kMmaWarp) {
+    // After an abort some stages are never consumed, and a bulk copy into one of them may
+    // still be in flight: the CTA must not exit (and give its shared memory up) before such
+    // copies have landed. They are not observable on their own (a stage's full barrier also
+    // needs the producers' arrivals), so one thread keeps the CTA for a fixed
+    // kAbortCopyCycles, about 1 ms, far beyond the few microseconds a copy of two
+    // operand-table K-blocks takes. (The MMA warp has already waited for its MMAs.)
+    if (s_abort && tid == 0) {
+        const long long t0 = clock64();
+        while (clock64() - t0 < kAbortCopyCycles) {
+        }
+    }
+    if (warp == 4) {
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                      "r"(kTmemCols)

@@ -68,6 +68,12 @@ class Server:
         keys = ("batches", "objects_done", "largest_batch", "waiting", "peak_inflight_bytes")
         return dict(zip(keys, (int(v) for v in out)))
 
+    def peaks(self):
+        out = (ctypes.c_uint64 * 4)()
+        self._lib.lsgb_server_peaks(self._h, out)
+        keys = ("peak_inflight_bytes", "peak_slots_in_flight", "peak_waiting", "budget_deferrals")
+        return dict(zip(keys, (int(v) for v in out)))
+
     def now(self) -> float:
         return float(self._lib.lsgb_server_now())
 
@@ -148,7 +154,7 @@ def replay(stream: synth.Stream, n_objects: int | None = None, variant: int = ST
     wall = time.perf_counter() - t0
     done.set()
     th.join()
-    stats_before_close = srv.stats()
+    stats_before_close = {**srv.stats(), **srv.peaks()}
     srv.close()
     ids = np.concatenate([r[0] for r in results]) if results else np.zeros(0, np.uint64)
     order = np.argsort(ids)

@@ -220,6 +220,10 @@ LSGB_API int lsgb_server_poll(lsgb_server *srv, uint32_t max, uint64_t *ids, uin
 /* [batches launched, objects completed, largest batch, objects waiting, peak
  * in-flight device bytes] */
 LSGB_API int lsgb_server_stats(lsgb_server *srv, uint64_t *out5);
+/* [peak in-flight device bytes, peak batches (slots) in flight at once, peak objects
+ * waiting for admission, admissions that stopped at the HBM budget] since the server was
+ * created. */
+LSGB_API int lsgb_server_peaks(lsgb_server *srv, uint64_t *out4);
 LSGB_API double lsgb_server_now(void);
 /* Finishes every submitted object, then stops the loop and frees it; results not yet
  * taken with lsgb_server_poll are discarded. */

@@ -8,8 +8,8 @@ around every object's best index:
   * plain FP64 <= 1e-9 relative (tests/gpu_helpers.py);
   * each GPU best index is the oracle's maximum over its window and over the sample,
     within the tolerance.
-On the long object the mixed form's re-anchoring interval R is swept over 16, 64 and
-256 (0 = every thread's run re-anchors, the production setting). The errors are
+On the long object the CUDA-core mixed form's re-anchoring interval R is swept over 16, 64
+and 256, each held to the same bar (0 = the production setting, the tensor form). The errors are
 written to $LSGB_PRECISION_REPORT (JSON) when that variable is set.
 """
 import json
@@ -78,6 +78,7 @@ def _check(name, eng, w, variant, precision, n_sample=600, seed=0):
         r, _ = pyoracle.batch_pgram(variant, w.t[a:b], y[a:b], w.dy[a:b], [0, b - a], w.fmin, w.df,
                                     kidx=wk[o])
         wref[o] = r[0]
+    extra = {}
     if precision == "mixed":
         err = max(float(np.max(np.abs(cols - ref))), float(np.max(np.abs(wpow - wref))))
         ok = err < MIXED_ATOL
@@ -86,6 +87,15 @@ def _check(name, eng, w, variant, precision, n_sample=600, seed=0):
         err = max(plain_rel_err(cols, ref), plain_rel_err(wpow, wref))
         ok = err < PLAIN_RTOL
         tol = 0.0
+        # the same without the floor (relative to each power however small), and where
+        # the largest one is: the floor only matters for powers that are cancellations
+        rel = np.abs(cols - ref) / np.abs(ref)
+        o, j = np.unravel_index(int(np.argmax(rel)), rel.shape)
+        extra = {"max_rel_err_unfloored": float(rel[o, j]),
+                 "at_power_over_peak": float(abs(ref[o, j]) / np.max(np.abs(ref[o]))),
+                 "max_rel_err_unfloored_above_1e-3_peak": float(np.max(
+                     np.where(np.abs(ref) >= 1e-3 * np.max(np.abs(ref), axis=1, keepdims=True),
+                              rel, 0.0)))}
     center = 8
     bad = 0
     for o in range(w.n_obj):
@@ -94,7 +104,7 @@ def _check(name, eng, w, variant, precision, n_sample=600, seed=0):
             bad += 1
     REPORT[name] = {"precision": precision, "max_err": err, "objects": w.n_obj,
                     "n_freq": w.n_freq, "sampled_freqs": int(kidx.size), "best_mismatch": bad,
-                    "metric": "abs" if precision == "mixed" else "rel"}
+                    "metric": "abs" if precision == "mixed" else "rel (floored)", **extra}
     print(name, REPORT[name])
     assert ok, (name, err)
     assert bad == 0, (name, bad)
@@ -124,16 +134,12 @@ def test_lognormal_batch_generalized(eng, precision):
 
 @pytest.mark.parametrize("reanchor", [0, 16, 64, 256])
 def test_long_object_reanchor_sweep(eng, reanchor):
+    """Every interval R of the sweep must meet the mixed bar (1e-4) with identical best
+    periods; R = 0 is the production setting (the default tensor form)."""
     w = synth.long_object()
     eng.set_reanchor(reanchor)
     try:
-        name = f"long_200kobs_1e7f_mixed_R{reanchor or 'F'}"
-        if reanchor == 0:
-            _check(name, eng, w, 0, "mixed", n_sample=400, seed=3)
-        else:
-            try:
-                _check(name, eng, w, 0, "mixed", n_sample=400, seed=3)
-            except AssertionError:
-                pass  # recorded in the report; only the production setting must meet 1e-4
+        _check(f"long_200kobs_1e7f_mixed_R{reanchor or 'F'}", eng, w, 0, "mixed", n_sample=400,
+               seed=3)
     finally:
         eng.set_reanchor(0)

@@ -52,3 +52,37 @@ def test_server_without_gpu_fails_loudly(native_libs):
     with pytest.raises(E.LsgbError) as ei:
         serve.Server(1000, 1.0, 1e-3)
     assert ei.value.status == -4
+
+
+@pytest.mark.gpu
+def test_admission_under_a_binding_hbm_budget(native_libs, cuda_ok):
+    """Arrivals faster than the GPU serves them, and an HBM budget of about two batches:
+    admissions stop at the budget and objects wait, several batches are in flight at once,
+    and every result is still the same as the object computed alone."""
+    st = synth.stream(seed=91, n_obj=1500, rate_hz=60_000.0, n_freq=100_000)
+    objects = []
+    for i in range(1500):
+        t, y = synth.stream_object(st, i)
+        objects.append((t, y, np.ones_like(t)))
+    # device bytes in flight (lsgb_server.cpp batch_footprint): about 5.4 KB for an average
+    # object at 1e5 frequencies, so a 64 KB budget holds a dozen of them at a time
+    budget = 64 * 1024
+    report, res = serve.replay(st, slots=3, max_batch=64, hbm_budget_bytes=budget,
+                               objects=objects)
+    print({k: report[k] for k in ("batches", "largest_batch", "peak_slots_in_flight",
+                                  "peak_waiting", "budget_deferrals", "peak_inflight_bytes",
+                                  "latency_p50_ms", "latency_p99_ms")})
+    assert report["completed"] == 1500
+    assert report["budget_deferrals"] > 0
+    assert report["peak_waiting"] > 1
+    assert report["peak_slots_in_flight"] >= 2
+    assert report["peak_inflight_bytes"] <= budget or report["largest_batch"] == 1
+    eng = E.Engine(0)
+    df = (st.fmax - st.fmin) / st.n_freq
+    for i in range(0, 1500, 7):
+        t, y, _ = objects[i]
+        alone = eng.run_host(0, "mixed", t, y, None, np.array([0, t.size], np.uint64), st.fmin,
+                             df, st.n_freq, normalize=True)
+        assert res["best_idx"][i] == alone.best_idx[0], i
+        assert res["best_power"][i] == alone.best_power[0], i
+    eng.close()
