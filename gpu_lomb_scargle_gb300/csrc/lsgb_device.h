@@ -60,6 +60,14 @@ __device__ __forceinline__ unsigned long long rank_key(float p, uint32_t k) {
 // A thread's or warp's three largest keys, t0 > t1 > t2 (0 = empty).
 struct Top3 {
     unsigned long long t0 = 0ull, t1 = 0ull, t2 = 0ull;
+    float floor2 = 0.0f;  // the power of t2: a smaller power can never enter
+    // Starts from a known lower bound g (the object's current third key, which only grows):
+    // keys not above g could never be inserted and are not kept. The triple then holds
+    // copies of g below the keys that beat it; g itself is never offered again.
+    __device__ __forceinline__ void seed(unsigned long long g) {
+        t0 = t1 = t2 = g;
+        floor2 = __uint_as_float((uint32_t)(g >> 32));
+    }
     // Offers a key (keys offered to one Top3 are distinct).
     __device__ __forceinline__ void offer(unsigned long long x) {
         if (x > t2) {
@@ -70,11 +78,25 @@ struct Top3 {
             } else {
                 t2 = x;
             }
+            floor2 = __uint_as_float((uint32_t)(t2 >> 32));
         }
     }
-    // Offers a positive power at frequency index k.
+    // Offers a positive power at frequency index k; one float compare for the powers below
+    // the current third (an equal power may still enter, with a lower index).
     __device__ __forceinline__ void offer(float p, uint32_t k) {
-        if (p > 0.0f) offer(rank_key(p, k));
+        if (p > 0.0f && p >= floor2) offer(rank_key(p, k));
+    }
+    // Offers n powers p[i] at indices k0 + i * step behind one branch on their maximum,
+    // which after the first few is almost always below the floor.
+    template <int n>
+    __device__ __forceinline__ void offer_run(const float (&p)[n], uint32_t k0, uint32_t step) {
+        float m = p[0];
+#pragma unroll
+        for (int i = 1; i < n; ++i) m = fmaxf(m, p[i]);
+        if (m > 0.0f && m >= floor2) {
+#pragma unroll
+            for (int i = 0; i < n; ++i) offer(p[i], k0 + step * (uint32_t)i);
+        }
     }
     // Merges the three keys of every lane of the (converged) warp into every lane. The
     // butterfly pairs disjoint groups of lanes, so the keys merged are always distinct.

@@ -84,12 +84,14 @@ void two_prod(double a, double b_hi, double b_lo, double &hi, double &lo) {
 struct Workspace {
     DevBuf objs, offs, perm, rec, tile_best, counter, keys;
     DevBuf optab;  // tensor form: per-K-block left operands and steps (tensor_optab_bytes)
+    DevBuf partial;  // tensor form with K slices: each unit's raw sums (tensor_partial_bytes)
     // sticky status word of the call's kernels (kStatusTimeout: a bounded pipeline wait of
     // the tensor form ran out; kStatusBadInput: non-finite or invalid inputs); zeroed when
     // allocated and after it is reported
     DevBuf status;
     void release() {
-        DevBuf *b[] = {&objs, &offs, &perm, &rec, &tile_best, &counter, &keys, &optab, &status};
+        DevBuf *b[] = {&objs, &offs, &perm, &rec, &tile_best, &counter, &keys, &optab, &partial,
+                       &status};
         for (DevBuf *x : b) x->release();
     }
 };
@@ -104,6 +106,7 @@ struct Batch {
     uint32_t n_obj = 0, n_freq = 0, n_tiles = 0, max_n = 0, chunk = 0;
     uint64_t rows = 0, units = 0;
     uint64_t total_kb = 0;  // tensor form: K-blocks of the batch (operand table entries)
+    uint32_t ksplit = 1;    // tensor form: slices of every object's K-blocks (units = pairs x ksplit)
     double fmin = 0, df = 0;
     MixedShape shape{};
     uint32_t reanchor = 0;
@@ -205,6 +208,18 @@ int plan_batch(Batch &b, int sms, const MixedShape *shapes, uint32_t reanchor, i
         }
         if (kb >= 0xffffffffull) return fail(LSGB_ERR_INVALID, "batch too long for the tensor form");
         b.total_kb = kb;
+        // Fewer (object, tile) pairs than SMs: cut every object's K-blocks into slices so
+        // that the units fill the SMs, each slice at least kMinSliceKB K-blocks long; a
+        // finishing pass adds the slices' sums (one object of 3,555 observations and 1e5
+        // frequencies: 13 pairs, 11 slices)
+        b.ksplit = 1;
+        const uint32_t min_nkb = (b.objs[b.perm.back()].n + kTensorKBlock - 1) / kTensorKBlock;
+        if (b.units < (uint64_t)sms) {
+            const uint64_t by_sms = (uint64_t)sms / b.units;
+            const uint64_t by_len = min_nkb / kMinSliceKB;
+            b.ksplit = (uint32_t)std::max<uint64_t>(1, std::min(by_sms, by_len));
+        }
+        b.units *= b.ksplit;
     } else if (mixed) {
         // Shared memory per CTA: at most what keeps the CTAs per SM that the shape's
         // register budget allows resident (less the per-CTA reservation and the static
@@ -250,6 +265,8 @@ int upload_tables(const Batch &b, Workspace &ws, cudaStream_t st) {
         LSGB_CUDA(ws.keys.ensure(sizeof(unsigned long long) * b.n_obj * b.top));
     if (mixed) LSGB_CUDA(ws.rec.ensure(mixed_global_rec_bytes(b.shape) * b.rows));
     if (mixed && b.shape.x2 == 3) LSGB_CUDA(ws.optab.ensure(tensor_optab_bytes(b.variant, b.total_kb)));
+    if (mixed && b.shape.x2 == 3 && b.ksplit > 1)
+        LSGB_CUDA(ws.partial.ensure(tensor_partial_bytes(b.variant) * b.units));
     if (!ws.status.p) {
         LSGB_CUDA(ws.status.ensure(sizeof(uint32_t)));
         LSGB_CUDA(cudaMemsetAsync(ws.status.p, 0, sizeof(uint32_t), st));
@@ -347,6 +364,8 @@ int enqueue_batch(Batch &b, Workspace &ws, cudaStream_t st, cudaEvent_t ev0, cud
         a.status = (uint32_t *)ws.status.p;
         a.top = b.top;
         a.wait_cycles = b.wait_cycles;
+        a.ksplit = b.ksplit;
+        a.partial = b.ksplit > 1 ? (float *)ws.partial.p : nullptr;
         if (b.shape.x2 == 3) {
             LSGB_CUDA(launch_tensor_optab(b.variant, a, b.total_kb, st));
             ++kernels;

@@ -102,6 +102,10 @@ struct MixedArgs {
     uint32_t total_kb;     // tensor form: K-blocks of the batch (the table's phase stride)
     uint32_t top;          // best frequencies kept per object: 1 (argmax) or 3
     long long wait_cycles; // tensor form: limit of a bounded pipeline wait (0: the default)
+    uint32_t ksplit;       // tensor form: slices of every object's K-blocks (0 or 1: none);
+                           // with slices, a unit's raw sums go to `partial` and a finishing
+                           // pass forms the powers
+    float *partial;        // tensor form with ksplit > 1: [units x tensor_partial_bytes]
 };
 
 
@@ -173,8 +177,13 @@ cudaError_t launch_tensor(int variant, int dtype, const MixedArgs &a, int grid, 
 // records. total_kb = sum over objects of ceil(n / 16); ObjInfo::kb0 must hold the prefix
 // sums.
 constexpr uint32_t kTensorKBlock = 16;
+// Shortest K slice (K-blocks) a batch with fewer (object, tile) pairs than SMs is cut into:
+// two of the kernel's 8-K-block passes, so that a unit's fixed costs (pipeline start, the
+// store of its raw sums) stay small beside its MMAs.
+constexpr uint32_t kMinSliceKB = 16;
 size_t tensor_step_bytes(int variant);
 size_t tensor_optab_bytes(int variant, uint64_t total_kb);
+size_t tensor_partial_bytes(int variant);  // raw sums of one split unit
 cudaError_t launch_tensor_optab(int variant, const MixedArgs &a, uint64_t total_kb, cudaStream_t st);
 // Compiled mixed shapes as (variant, F, threads, min CTAs, packed, unroll); returns the count.
 int mixed_shapes(int *out, int max_shapes);

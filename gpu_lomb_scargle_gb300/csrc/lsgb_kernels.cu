@@ -593,8 +593,12 @@ __global__ void __launch_bounds__(NT, MINB) mixed_kernel(MixedArgs a) {
         float bp = 0.0f;
         uint32_t bk = 0xffffffffu;
         if (tile == 0 && threadIdx.x == 0) bk = 0;  // the reference's (power 0, index 0) start
-        const bool top3 = a.top == 3u;  // keep the three best instead of the maximum
+        const bool top3 = a.top == 3u && a.best_key;  // the three best, not the maximum
+        // the object's current third key: whatever is not above it is dropped here
+        const unsigned long long g3 =
+            top3 ? *(volatile unsigned long long *)(a.best_key + 3ull * o + 2) : 0ull;
         Top3 t3;
+        t3.seed(g3);
         const uint64_t out0 = (uint64_t)o * a.n_freq;
         const float nrm = a.objs[o].norm32;
         if (!GEN) {
@@ -624,10 +628,11 @@ __global__ void __launch_bounds__(NT, MINB) mixed_kernel(MixedArgs a) {
                 }
             }
         }
-        if (a.best_key && top3) {
-            // the warp's three best, then into the object's three slots
-            t3.warp_merge();
-            if ((threadIdx.x & 31) == 0) {
+        if (top3) {
+            // the warp's three best, then into the object's three slots; a warp none of whose
+            // lanes beat the seed has nothing to insert
+            if (__any_sync(0xffffffffu, t3.t0 > g3)) t3.warp_merge();
+            if ((threadIdx.x & 31) == 0 && t3.t0 > g3) {
                 unsigned long long *slots = a.best_key + 3ull * o;
                 top3_insert(slots, t3.t0);
                 top3_insert(slots, t3.t1);

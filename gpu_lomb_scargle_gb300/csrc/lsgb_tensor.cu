@@ -348,20 +348,39 @@ __device__ __forceinline__ void turn_sincos(uint32_t hi, float &s, float &c) {
     __sincosf((float)(int32_t)hi * kTwoPiOver2p32f, &s, &c);
 }
 
+// Work units: (object, frequency tile) pairs q in queue order, each cut into S = ksplit
+// slices of its object's K-blocks (S = 1 unless the batch has fewer pairs than SMs); unit
+// u = q S + s sums slice s, K-blocks [nkb s / S, nkb (s + 1) / S) of the object.
+__device__ __forceinline__ uint32_t ksplit_of(const MixedArgs &a) {
+    return a.ksplit > 1u ? a.ksplit : 1u;
+}
+
 struct UnitInfo {
-    uint32_t o, tile, n, nkb, kb0;
+    uint32_t o, tile, n, nkb, kb0;  // n: the object's observations; nkb, kb0: the slice's
+    uint32_t u;
     uint64_t row0;
 };
 
 __device__ __forceinline__ UnitInfo unit_info_of(const MixedArgs &a, uint32_t u, uint32_t o) {
     UnitInfo w;
+    const uint32_t S = ksplit_of(a);
+    const uint32_t q = u / S, s = u - q * S;
     w.o = o;
-    w.tile = u % a.n_tiles;
+    w.u = u;
+    w.tile = q % a.n_tiles;
     w.row0 = a.objs[o].row0;
     w.n = a.objs[o].n;
-    w.kb0 = a.objs[o].kb0;
-    w.nkb = (w.n + kTK - 1) / kTK;
+    const uint32_t nkb = (w.n + kTK - 1) / kTK;
+    const uint32_t b0 = (uint32_t)((uint64_t)nkb * s / S);
+    const uint32_t b1 = (uint32_t)((uint64_t)nkb * (s + 1u) / S);
+    w.kb0 = a.objs[o].kb0 + b0;
+    w.nkb = b1 - b0;
     return w;
+}
+
+// The object of unit u.
+__device__ __forceinline__ uint32_t unit_obj(const MixedArgs &a, uint32_t u) {
+    return a.perm[u / (a.n_tiles * ksplit_of(a))];
 }
 
 // A CTA's walk over its units b, b + g, b + 2g, ... (b = blockIdx.x, g = gridDim.x) with
@@ -374,14 +393,14 @@ struct UnitWalk {
     uint32_t o1;  // object of the unit after the one in nxt
     __device__ __forceinline__ UnitWalk(const MixedArgs &a, uint32_t units) {
         const uint32_t b = blockIdx.x, g = gridDim.x;
-        if (b < units) nxt = unit_info_of(a, b, a.perm[b / a.n_tiles]);
-        o1 = b + g < units ? a.perm[(b + g) / a.n_tiles] : 0u;
+        if (b < units) nxt = unit_info_of(a, b, unit_obj(a, b));
+        o1 = b + g < units ? unit_obj(a, b + g) : 0u;
     }
     __device__ __forceinline__ UnitInfo next(const MixedArgs &a, uint32_t u, uint32_t units) {
         const UnitInfo cur = nxt;
         const uint32_t u1 = u + gridDim.x, u2 = u1 + gridDim.x;
         if (u1 < units) nxt = unit_info_of(a, u1, o1);
-        o1 = u2 < units ? a.perm[u2 / a.n_tiles] : 0u;
+        o1 = u2 < units ? unit_obj(a, u2) : 0u;
         return cur;
     }
 };
@@ -412,6 +431,41 @@ struct SlotRing {
     }
 };
 
+// The powers of two frequencies (packed pairs) from their raw sums in TMEM order, standard
+// (XC, XS, C2, S2) and generalized (C, S, YC, YS, C2, S2), with the object's scales.
+template <bool GEN>
+struct SumPower {
+    uint64_t NN, NN2, FA, FB, S0, S1, NYB, NRM;
+    __device__ __forceinline__ SumPower(float nrm, float tsc0, float tsc1, float invw, float ybar,
+                                        uint32_t n) {
+        const float us0 = 1.0f / tsc0, us1 = 1.0f / tsc1;  // powers of two
+        // standard: P = (2P of the raw sums) us0 (us0 nrm / 2), the scale applied in two
+        // steps so that us0^2 never forms; generalized: weight-normalized sums
+        const float fa = us0, fb = 0.5f * nrm * us0;
+        const float s0 = us0 * invw, s1 = us1 * invw;
+        const float Nf = (float)n, N2 = Nf * Nf;
+        NN = pack2(Nf, Nf);
+        NN2 = pack2(N2, N2);
+        FA = pack2(fa, fa);
+        FB = pack2(fb, fb);
+        S0 = pack2(s0, s0);
+        S1 = pack2(s1, s1);
+        NYB = pack2(-ybar, -ybar);
+        NRM = pack2(nrm, nrm);
+    }
+    __device__ __forceinline__ uint64_t operator()(uint64_t q0, uint64_t q1, uint64_t q2,
+                                                   uint64_t q3, uint64_t q4, uint64_t q5) const {
+        if (GEN) {
+            const uint64_t cb = fmul2(q0, S0), sb = fmul2(q1, S0);
+            return fmul2(gen_power_sums2(cb, sb, ffma2(NYB, cb, fmul2(q2, S1)),
+                                         ffma2(NYB, sb, fmul2(q3, S1)), fmul2(q4, S0),
+                                         fmul2(q5, S0)),
+                         NRM);
+        }
+        return fmul2(fmul2(std_power2_sums2(NN, NN2, q0, q1, q2, q3), FA), FB);
+    }
+};
+
 template <bool GEN, typename OutT>
 __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
     using G = TGeo<GEN>;
@@ -430,7 +484,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
     __shared__ volatile uint32_t s_abort;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint32_t units = a.n_obj * a.n_tiles;
+    const uint32_t units = a.n_obj * a.n_tiles * ksplit_of(a);
     const long long lim = a.wait_cycles > 0 ? a.wait_cycles : kWaitCycles;  // pipeline waits
 
     if (tid == 0) {
@@ -663,7 +717,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             uint32_t rsum[2] = {0u, 0u};  // the unit's running-sum slots
             UnitWalk walk(a, units);
             for (uint32_t u = blockIdx.x; u < units && ok; u += gridDim.x) {
-                const UnitInfo w = walk.next(a, u, units);  // nkb >= 1: no object is empty
+                const UnitInfo w = walk.next(a, u, units);  // nkb >= 1: no slice is empty
                 for (uint32_t ph = 0; ph < 2 && ok; ++ph) {
                     for (uint32_t kb0 = 0; kb0 < w.nkb && ok; kb0 += kPassKB) {
                         uint32_t sp;
@@ -815,21 +869,19 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             const uint32_t run1 = tmem + lane_base + rsum[0] * kSlotCols;
             const uint32_t run2 = tmem + lane_base + rsum[1] * kSlotCols;
             const uint32_t kT = w.tile * (uint32_t)G::TILE;
-            const float us0 = 1.0f / tsc0, us1 = 1.0f / tsc1;  // powers of two
-            // standard: P = (2P of the raw sums) us0 (us0 nrm / 2), the scale applied in
-            // two steps so that us0^2 never forms; generalized: weight-normalized sums
-            const float fa = us0, fb = 0.5f * nrm * us0;
-            const float s0 = us0 * invw, s1 = us1 * invw;
-            const float Nf = (float)w.n, N2 = Nf * Nf;
-            const uint64_t NN = pack2(Nf, Nf), NN2 = pack2(N2, N2), FA = pack2(fa, fa), FB = pack2(fb, fb);
-            const uint64_t S0 = pack2(s0, s0), S1 = pack2(s1, s1), NYB = pack2(-ybar, -ybar);
-            const uint64_t NRM = pack2(nrm, nrm);
+            const SumPower<GEN> power2(nrm, tsc0, tsc1, invw, ybar, w.n);
             const uint64_t out0 = (uint64_t)w.o * a.n_freq;
             float bp = 0.0f;
             uint32_t bk = 0xffffffffu;
             if (w.tile == 0 && pl == 0 && eh == 0) bk = 0;  // the reference's (power 0, index 0) start
-            const bool top3 = a.top == 3u;  // keep the three best instead of the maximum
+            // split units store their raw sums for ksum_kernel instead of powers
+            const bool split = a.ksplit > 1u;
+            const bool top3 = a.top == 3u && a.best_key && !split;  // the three best
+            // the object's current third key: whatever is not above it is dropped here
+            const unsigned long long g3 =
+                top3 ? *(volatile unsigned long long *)(a.best_key + 3ull * w.o + 2) : 0ull;
             Top3 t3;
+            t3.seed(g3);
             // quantities: phase 0 groups (re, im) then phase 1 (re, im)
             constexpr int NQ = GEN ? 6 : 4;
             // frequencies per chunk: 16 for the standard variant (eight independent packed
@@ -854,6 +906,18 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             for (int m0 = mbeg; m0 < mend; m0 += CHK) {
                 load_chunk(m0);
                 tmem_wait_ld();
+                if (split) {
+                    // [unit][quantity][p + 128 m]: a warp's stores are 128 contiguous bytes
+                    float *dst = a.partial + (uint64_t)w.u * (uint32_t)(NQ * G::TILE) + pl +
+                                 (uint32_t)kTP * (uint32_t)m0;
+#pragma unroll
+                    for (int k = 0; k < NQ; ++k)
+#pragma unroll
+                        for (int i = 0; i < CHK; ++i)
+                            __stcg(dst + (uint32_t)k * (uint32_t)G::TILE + (uint32_t)kTP * (uint32_t)i,
+                                   __uint_as_float(x[k][i]));
+                    continue;
+                }
                 float q[NQ][CHK];
 #pragma unroll
                 for (int k = 0; k < NQ; ++k)
@@ -865,20 +929,8 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                 auto power_at = [&](int i) {
                     if ((i & 1) != 0) return;
                     auto pq = [&](int k) { return pack2(q[k][i], q[k][i + 1]); };
-                    if (GEN) {
-                        const uint64_t cb = fmul2(pq(0), S0), sb = fmul2(pq(1), S0);
-                        const uint64_t p2 = fmul2(
-                            gen_power_sums2(cb, sb, ffma2(NYB, cb, fmul2(pq(2), S1)),
-                                            ffma2(NYB, sb, fmul2(pq(3), S1)), fmul2(pq(4), S0),
-                                            fmul2(pq(5), S0)),
-                            NRM);
-                        unpack2(p2, P[i], P[i + 1]);
-                    } else {
-                        const uint64_t p2 = fmul2(
-                            fmul2(std_power2_sums2(NN, NN2, pq(0), pq(1), pq(2), pq(3)), FA),
-                            FB);
-                        unpack2(p2, P[i], P[i + 1]);
-                    }
+                    unpack2(power2(pq(0), pq(1), pq(2), pq(3), pq(GEN ? 4 : 0), pq(GEN ? 5 : 0)),
+                            P[i], P[i + 1]);
                 };
 #pragma unroll
                 for (int i = 0; i < CHK; ++i) power_at(i);
@@ -892,8 +944,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                         for (int i = 0; i < CHK; ++i) store_out<OutT>(a.pgram, out0 + k0 + (uint32_t)kTP * (uint32_t)i, P[i]);
                     }
                     if (top3) {
-#pragma unroll
-                        for (int i = 0; i < CHK; ++i) t3.offer(P[i], k0 + (uint32_t)kTP * (uint32_t)i);
+                        t3.offer_run(P, k0, (uint32_t)kTP);
                     } else {
 #pragma unroll
                         for (int i = 0; i < CHK; ++i)
@@ -920,16 +971,17 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             }
             ring.push(rsum[0]);
             ring.push(rsum[1]);
-            if (a.best_key && top3) {
-                // the warp's three best, then into the object's three slots
-                t3.warp_merge();
-                if (lane == 0) {
+            if (top3) {
+                // the warp's three best, then into the object's three slots; a warp none of
+                // whose lanes beat the seed has nothing to insert
+                if (__any_sync(0xffffffffu, t3.t0 > g3)) t3.warp_merge();
+                if (lane == 0 && t3.t0 > g3) {
                     unsigned long long *slots = a.best_key + 3ull * w.o;
                     top3_insert(slots, t3.t0);
                     top3_insert(slots, t3.t1);
                     top3_insert(slots, t3.t2);
                 }
-            } else if (a.best_key) {
+            } else if (a.best_key && !split) {
 #pragma unroll
                 for (int off = 16; off > 0; off >>= 1) {
                     const float op = __shfl_xor_sync(0xffffffffu, bp, off);
@@ -962,6 +1014,76 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                      "r"(kTmemCols)
                      : "memory");
+    }
+}
+
+// The finishing pass of split units: for each (object, tile) pair q and frequency of the
+// tile, the S slices' raw sums added in FP32 in slice order, then the power, the
+// periodogram store and the object's best frequencies as the tensor kernel's epilogue
+// forms them. A thread takes two consecutive frequencies of one tile.
+constexpr uint32_t kKsumFreqs = 512;  // frequencies per CTA (256 threads)
+
+template <bool GEN, typename OutT>
+__global__ void __launch_bounds__(256) ksum_kernel(MixedArgs a) {
+    using G = TGeo<GEN>;
+    constexpr int NQ = GEN ? 6 : 4;
+    constexpr uint32_t CPT = (uint32_t)G::TILE / kKsumFreqs;  // CTAs per tile
+    const uint32_t S = ksplit_of(a);
+    const uint32_t q = blockIdx.x / CPT;
+    const uint32_t f = (blockIdx.x - q * CPT) * kKsumFreqs + 2u * threadIdx.x;
+    const uint32_t o = a.perm[q / a.n_tiles];
+    const uint32_t k0 = (q % a.n_tiles) * (uint32_t)G::TILE + f;
+    const ObjInfo &ob = a.objs[o];
+    const SumPower<GEN> power2(ob.norm32, ob.tsc0, ob.tsc1, ob.invw32, ob.ybar32, ob.n);
+    float2 v[NQ];
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) v[k] = make_float2(0.0f, 0.0f);
+    const float *src = a.partial + (uint64_t)q * S * (uint32_t)(NQ * G::TILE) + f;
+    for (uint32_t s = 0; s < S; ++s, src += NQ * G::TILE) {
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) {
+            const float2 x = __ldcg(reinterpret_cast<const float2 *>(src + k * G::TILE));
+            v[k].x += x.x;
+            v[k].y += x.y;
+        }
+    }
+    auto pv = [&](int k) { return pack2(v[k].x, v[k].y); };
+    float P[2];
+    unpack2(power2(pv(0), pv(1), pv(2), pv(3), pv(GEN ? 4 : 0), pv(GEN ? 5 : 0)), P[0], P[1]);
+    const uint64_t out0 = (uint64_t)o * a.n_freq;
+    const bool top3 = a.top == 3u && a.best_key;
+    const unsigned long long g3 =
+        top3 ? *(volatile unsigned long long *)(a.best_key + 3ull * o + 2) : 0ull;
+    Top3 t3;
+    t3.seed(g3);
+    float bp = 0.0f;
+    uint32_t bk = 0xffffffffu;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const uint32_t k = k0 + (uint32_t)i;
+        if (k < a.n_freq) {
+            if (a.pgram) store_out<OutT>(a.pgram, out0 + k, P[i]);
+            if (top3) t3.offer(P[i], k);
+            else if (P[i] > bp) { bp = P[i]; bk = k; }
+        }
+    }
+    if (top3) {
+        if (__any_sync(0xffffffffu, t3.t0 > g3)) t3.warp_merge();
+        if ((threadIdx.x & 31u) == 0 && t3.t0 > g3) {
+            unsigned long long *slots = a.best_key + 3ull * o;
+            top3_insert(slots, t3.t0);
+            top3_insert(slots, t3.t1);
+            top3_insert(slots, t3.t2);
+        }
+    } else if (a.best_key) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const float op = __shfl_xor_sync(0xffffffffu, bp, off);
+            const uint32_t ok2 = __shfl_xor_sync(0xffffffffu, bk, off);
+            if (better(op, ok2, bp, bk)) { bp = op; bk = ok2; }
+        }
+        if ((threadIdx.x & 31u) == 0 && bp > 0.0f)
+            atomicMax(a.best_key + o, rank_key(bp, bk));
     }
 }
 
@@ -1086,9 +1208,27 @@ cudaError_t launch_tensor_optab(int variant, const MixedArgs &a, uint64_t total_
 }
 
 cudaError_t launch_tensor(int variant, int dtype, const MixedArgs &a, int grid, cudaStream_t st) {
+    cudaError_t e;
     if (variant == 0)
-        return dtype == 0 ? launch_t<false, float>(a, grid, st) : launch_t<false, double>(a, grid, st);
-    return dtype == 0 ? launch_t<true, float>(a, grid, st) : launch_t<true, double>(a, grid, st);
+        e = dtype == 0 ? launch_t<false, float>(a, grid, st) : launch_t<false, double>(a, grid, st);
+    else
+        e = dtype == 0 ? launch_t<true, float>(a, grid, st) : launch_t<true, double>(a, grid, st);
+    if (e != cudaSuccess || a.ksplit <= 1u) return e;
+    // split units: the finishing pass over every (object, tile) pair
+    const uint64_t blocks = (uint64_t)a.n_obj * a.n_tiles * (tensor_tile_freqs(variant) / kKsumFreqs);
+    if (blocks > 0x7fffffffull) return cudaErrorInvalidValue;
+    if (variant == 0) {
+        if (dtype == 0) ksum_kernel<false, float><<<(unsigned)blocks, 256, 0, st>>>(a);
+        else ksum_kernel<false, double><<<(unsigned)blocks, 256, 0, st>>>(a);
+    } else {
+        if (dtype == 0) ksum_kernel<true, float><<<(unsigned)blocks, 256, 0, st>>>(a);
+        else ksum_kernel<true, double><<<(unsigned)blocks, 256, 0, st>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+size_t tensor_partial_bytes(int variant) {
+    return sizeof(float) * (variant ? 6u * (size_t)TGeo<true>::TILE : 4u * (size_t)TGeo<false>::TILE);
 }
 
 }  // namespace lsgb
