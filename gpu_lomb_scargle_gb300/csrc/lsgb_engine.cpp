@@ -751,7 +751,9 @@ static int periodogram_host(lsgb_engine *eng, int variant, int precision, int dt
     // A large periodogram goes out in object chunks: every chunk's computation is queued
     // first, then each chunk is copied to the host on a second stream as soon as it is
     // done, so the copy of chunk c overlaps the computation of chunks c+1.. (the result
-    // of an object does not depend on the batch it is computed in).
+    // of an object does not depend on the batch it is computed in, unless a batch has fewer
+    // (object, tile) pairs than SMs: the tensor form then sums K slices, in another order,
+    // within the mixed form's tolerance).
     const size_t kChunkBytes = size_t(512) << 20;
     const uint32_t n_chunks =
         (d_pg && n_freq && es * pg_elems > kChunkBytes && n_obj >= 2)

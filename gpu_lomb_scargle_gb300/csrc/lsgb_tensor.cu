@@ -349,10 +349,12 @@ __device__ __forceinline__ void turn_sincos(uint32_t hi, float &s, float &c) {
 }
 
 // Work units: (object, frequency tile) pairs q in queue order, each cut into S = ksplit
-// slices of its object's K-blocks (S = 1 unless the batch has fewer pairs than SMs); unit
-// u = q S + s sums slice s, K-blocks [nkb s / S, nkb (s + 1) / S) of the object.
+// slices of its object's K-blocks when SPLIT (a batch with fewer pairs than SMs); unit
+// u = q S + s sums slice s of the object's nkb K-blocks: nkb / S of them, one more for the
+// first nkb % S slices. Without SPLIT, unit u is pair u.
+template <bool SPLIT>
 __device__ __forceinline__ uint32_t ksplit_of(const MixedArgs &a) {
-    return a.ksplit > 1u ? a.ksplit : 1u;
+    return SPLIT ? a.ksplit : 1u;
 }
 
 struct UnitInfo {
@@ -361,26 +363,32 @@ struct UnitInfo {
     uint64_t row0;
 };
 
+template <bool SPLIT>
 __device__ __forceinline__ UnitInfo unit_info_of(const MixedArgs &a, uint32_t u, uint32_t o) {
     UnitInfo w;
-    const uint32_t S = ksplit_of(a);
-    const uint32_t q = u / S, s = u - q * S;
     w.o = o;
     w.u = u;
-    w.tile = q % a.n_tiles;
     w.row0 = a.objs[o].row0;
     w.n = a.objs[o].n;
-    const uint32_t nkb = (w.n + kTK - 1) / kTK;
-    const uint32_t b0 = (uint32_t)((uint64_t)nkb * s / S);
-    const uint32_t b1 = (uint32_t)((uint64_t)nkb * (s + 1u) / S);
-    w.kb0 = a.objs[o].kb0 + b0;
-    w.nkb = b1 - b0;
+    w.kb0 = a.objs[o].kb0;
+    w.nkb = (w.n + kTK - 1) / kTK;
+    if (!SPLIT) {
+        w.tile = u % a.n_tiles;
+    } else {
+        const uint32_t S = a.ksplit;
+        const uint32_t q = u / S, s = u - q * S;
+        w.tile = q % a.n_tiles;
+        const uint32_t len = w.nkb / S, extra = w.nkb - len * S;
+        w.kb0 += len * s + min(s, extra);
+        w.nkb = len + (s < extra ? 1u : 0u);
+    }
     return w;
 }
 
 // The object of unit u.
+template <bool SPLIT>
 __device__ __forceinline__ uint32_t unit_obj(const MixedArgs &a, uint32_t u) {
-    return a.perm[u / (a.n_tiles * ksplit_of(a))];
+    return a.perm[SPLIT ? u / (a.n_tiles * a.ksplit) : u / a.n_tiles];
 }
 
 // A CTA's walk over its units b, b + g, b + 2g, ... (b = blockIdx.x, g = gridDim.x) with
@@ -388,19 +396,20 @@ __device__ __forceinline__ uint32_t unit_obj(const MixedArgs &a, uint32_t u) {
 // previous call, then issues the object loads of unit u + g (whose object index was read
 // one call earlier still) and the object index of unit u + 2g. No role then waits on the
 // perm -> objs load chain at a unit boundary.
+template <bool SPLIT>
 struct UnitWalk {
     UnitInfo nxt;
     uint32_t o1;  // object of the unit after the one in nxt
     __device__ __forceinline__ UnitWalk(const MixedArgs &a, uint32_t units) {
         const uint32_t b = blockIdx.x, g = gridDim.x;
-        if (b < units) nxt = unit_info_of(a, b, unit_obj(a, b));
-        o1 = b + g < units ? unit_obj(a, b + g) : 0u;
+        if (b < units) nxt = unit_info_of<SPLIT>(a, b, unit_obj<SPLIT>(a, b));
+        o1 = b + g < units ? unit_obj<SPLIT>(a, b + g) : 0u;
     }
     __device__ __forceinline__ UnitInfo next(const MixedArgs &a, uint32_t u, uint32_t units) {
         const UnitInfo cur = nxt;
         const uint32_t u1 = u + gridDim.x, u2 = u1 + gridDim.x;
-        if (u1 < units) nxt = unit_info_of(a, u1, o1);
-        o1 = u2 < units ? unit_obj(a, u2) : 0u;
+        if (u1 < units) nxt = unit_info_of<SPLIT>(a, u1, o1);
+        o1 = u2 < units ? unit_obj<SPLIT>(a, u2) : 0u;
         return cur;
     }
 };
@@ -466,7 +475,9 @@ struct SumPower {
     }
 };
 
-template <bool GEN, typename OutT>
+// SPLIT: the batch is K-sliced (the epilogue stores raw sums); TOP3: the three best
+// frequencies of each object instead of the maximum (launched with a.best_key set).
+template <bool GEN, typename OutT, bool SPLIT, bool TOP3>
 __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
     using G = TGeo<GEN>;
     constexpr int S = G::STAGES;
@@ -484,7 +495,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
     __shared__ volatile uint32_t s_abort;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint32_t units = a.n_obj * a.n_tiles * ksplit_of(a);
+    const uint32_t units = a.n_obj * a.n_tiles * ksplit_of<SPLIT>(a);
     const long long lim = a.wait_cycles > 0 ? a.wait_cycles : kWaitCycles;  // pipeline waits
 
     if (tid == 0) {
@@ -537,7 +548,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
         const uint32_t zo = (uint32_t)G::Z_OFF + hk * (uint32_t)G::ZKB + kmaj_off(m, j0);
         constexpr uint32_t kRowNM = (uint32_t)G::NM * 32u;  // kmaj_off(r + NM) - kmaj_off(r)
         uint32_t g = 0;
-        UnitWalk walk(a, units);
+        UnitWalk<SPLIT> walk(a, units);
         // the steps (and weights) of the group's K-block of the next stage, loaded one stage
         // ahead (only for K-blocks that exist)
         constexpr uint32_t NQ4 = JPT * (uint32_t)G::SB / 16u;  // uint4 per thread and stage
@@ -662,7 +673,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
         if (lane == 0) {
             const unsigned char *tab = static_cast<const unsigned char *>(a.optab);
             uint32_t g = 0;
-            UnitWalk walk(a, units);
+            UnitWalk<SPLIT> walk(a, units);
             const uint64_t tph = (uint64_t)a.total_kb * G::AKB;  // phase stride of the table
             auto prefetch = [&](uint32_t kbg, uint32_t n) {  // K-blocks kbg.. of both phases
                 bulk_prefetch_l2(tab + (uint64_t)kbg * G::AKB, n * (uint32_t)G::AKB);
@@ -715,7 +726,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             bool ok = true;
             SlotRing ring;
             uint32_t rsum[2] = {0u, 0u};  // the unit's running-sum slots
-            UnitWalk walk(a, units);
+            UnitWalk<SPLIT> walk(a, units);
             for (uint32_t u = blockIdx.x; u < units && ok; u += gridDim.x) {
                 const UnitInfo w = walk.next(a, u, units);  // nkb >= 1: no slice is empty
                 for (uint32_t ph = 0; ph < 2 && ok; ++ph) {
@@ -797,7 +808,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
         const uint32_t lane_base = (eq * 32u) << 16;
         bool ok = true;
         SlotRing ring;
-        UnitWalk walk(a, units);
+        UnitWalk<SPLIT> walk(a, units);
         for (uint32_t u = blockIdx.x; u < units && ok; u += gridDim.x) {
             const UnitInfo w = walk.next(a, u, units);
             // the object's fields for the power pass, loaded before the folds
@@ -875,8 +886,8 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             uint32_t bk = 0xffffffffu;
             if (w.tile == 0 && pl == 0 && eh == 0) bk = 0;  // the reference's (power 0, index 0) start
             // split units store their raw sums for ksum_kernel instead of powers
-            const bool split = a.ksplit > 1u;
-            const bool top3 = a.top == 3u && a.best_key && !split;  // the three best
+            constexpr bool split = SPLIT;
+            constexpr bool top3 = TOP3 && !SPLIT;
             // the object's current third key: whatever is not above it is dropped here
             const unsigned long long g3 =
                 top3 ? *(volatile unsigned long long *)(a.best_key + 3ull * w.o + 2) : 0ull;
@@ -906,7 +917,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             for (int m0 = mbeg; m0 < mend; m0 += CHK) {
                 load_chunk(m0);
                 tmem_wait_ld();
-                if (split) {
+                if constexpr (split) {
                     // [unit][quantity][p + 128 m]: a warp's stores are 128 contiguous bytes
                     float *dst = a.partial + (uint64_t)w.u * (uint32_t)(NQ * G::TILE) + pl +
                                  (uint32_t)kTP * (uint32_t)m0;
@@ -943,7 +954,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
 #pragma unroll
                         for (int i = 0; i < CHK; ++i) store_out<OutT>(a.pgram, out0 + k0 + (uint32_t)kTP * (uint32_t)i, P[i]);
                     }
-                    if (top3) {
+                    if constexpr (top3) {
                         t3.offer_run(P, k0, (uint32_t)kTP);
                     } else {
 #pragma unroll
@@ -956,7 +967,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                         const uint32_t k = k0 + (uint32_t)kTP * (uint32_t)i;
                         if (k < a.n_freq) {
                             if (a.pgram) store_out<OutT>(a.pgram, out0 + k, P[i]);
-                            if (top3) t3.offer(P[i], k);
+                            if constexpr (top3) t3.offer(P[i], k);
                             else if (P[i] > bp) { bp = P[i]; bk = k; }
                         }
                     }
@@ -971,7 +982,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             }
             ring.push(rsum[0]);
             ring.push(rsum[1]);
-            if (top3) {
+            if constexpr (top3) {
                 // the warp's three best, then into the object's three slots; a warp none of
                 // whose lanes beat the seed has nothing to insert
                 if (__any_sync(0xffffffffu, t3.t0 > g3)) t3.warp_merge();
@@ -981,7 +992,7 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
                     top3_insert(slots, t3.t1);
                     top3_insert(slots, t3.t2);
                 }
-            } else if (a.best_key && !split) {
+            } else if (!split && a.best_key) {
 #pragma unroll
                 for (int off = 16; off > 0; off >>= 1) {
                     const float op = __shfl_xor_sync(0xffffffffu, bp, off);
@@ -1028,7 +1039,7 @@ __global__ void __launch_bounds__(256) ksum_kernel(MixedArgs a) {
     using G = TGeo<GEN>;
     constexpr int NQ = GEN ? 6 : 4;
     constexpr uint32_t CPT = (uint32_t)G::TILE / kKsumFreqs;  // CTAs per tile
-    const uint32_t S = ksplit_of(a);
+    const uint32_t S = a.ksplit;
     const uint32_t q = blockIdx.x / CPT;
     const uint32_t f = (blockIdx.x - q * CPT) * kKsumFreqs + 2u * threadIdx.x;
     const uint32_t o = a.perm[q / a.n_tiles];
@@ -1171,7 +1182,9 @@ size_t tensor_smem() {
 
 template <bool GEN, typename OutT>
 cudaError_t launch_t(const MixedArgs &a, int grid, cudaStream_t st) {
-    auto k = tensor_kernel<GEN, OutT>;
+    void (*k)(MixedArgs) = tensor_kernel<GEN, OutT, false, false>;
+    if (a.ksplit > 1u) k = tensor_kernel<GEN, OutT, true, false>;  // ksum_kernel finishes
+    else if (a.top == 3u && a.best_key) k = tensor_kernel<GEN, OutT, false, true>;
     const size_t smem = tensor_smem<GEN>();
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

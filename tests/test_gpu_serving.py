@@ -1,5 +1,11 @@
 """The continuous-batching request loop: every object's result is the same alone and in
-the mix, and agrees with the oracle."""
+the mix, within the mixed form's tolerance, and agrees with the oracle.
+
+An object computed alone is a batch of few (object, frequency tile) pairs, which the tensor
+form cuts into K slices when the object has 512 or more observations; in a batch with more
+pairs than SMs it is not cut. The two sum in different orders, so their powers may differ in
+the last bits of FP32: the comparison is within MIXED_ATOL, and the best index is the same
+or a near-tie within it."""
 import numpy as np
 import pytest
 
@@ -7,6 +13,18 @@ from gpu_lomb_scargle_gb300 import engine as E
 from gpu_lomb_scargle_gb300 import serve, synth
 from oracle import pyoracle
 from tests.gpu_helpers import MIXED_ATOL
+
+
+def same_as_alone(res, i, alone, eng, variant, t, y, dy, st):
+    """Object i's result from the server against the same object computed alone."""
+    assert abs(res["best_power"][i] - alone.best_power[0]) <= MIXED_ATOL, i
+    if res["best_idx"][i] != alone.best_idx[0]:
+        # a near-tie: the alone periodogram's powers at the two indices are within the bar
+        df = (st.fmax - st.fmin) / st.n_freq
+        pg = eng.run_host(variant, "mixed", t, y, dy if variant else None,
+                          np.array([0, t.size], np.uint64), st.fmin, df, st.n_freq,
+                          normalize=True, want_pgram=True).pgram.reshape(-1)
+        assert abs(pg[res["best_idx"][i]] - pg[alone.best_idx[0]]) <= MIXED_ATOL, i
 
 
 @pytest.mark.gpu
@@ -29,8 +47,7 @@ def test_results_alone_equal_results_in_the_mix(native_libs, cuda_ok, variant):
                              np.array([0, t.size], np.uint64), st.fmin, df, st.n_freq,
                              normalize=True)
         assert res["ids"][i] == i
-        assert res["best_idx"][i] == alone.best_idx[0], i
-        assert res["best_power"][i] == alone.best_power[0], i
+        same_as_alone(res, i, alone, eng, variant, t, y, dy, st)
     # and a sample against the oracle (grid indices around each best and a coarse sweep)
     for i in range(0, 500, 50):
         t, y, dy = objects[i]
@@ -83,6 +100,5 @@ def test_admission_under_a_binding_hbm_budget(native_libs, cuda_ok):
         t, y, _ = objects[i]
         alone = eng.run_host(0, "mixed", t, y, None, np.array([0, t.size], np.uint64), st.fmin,
                              df, st.n_freq, normalize=True)
-        assert res["best_idx"][i] == alone.best_idx[0], i
-        assert res["best_power"][i] == alone.best_power[0], i
+        same_as_alone(res, i, alone, eng, 0, t, y, None, st)
     eng.close()
