@@ -85,13 +85,15 @@ struct Workspace {
     DevBuf objs, offs, perm, rec, tile_best, counter, keys;
     DevBuf optab;  // tensor form: per-K-block left operands and steps (tensor_optab_bytes)
     DevBuf partial;  // tensor form with K slices: each unit's raw sums (tensor_partial_bytes)
+    DevBuf kbobj;    // tensor form: the object of every K-block of the batch
+    DevBuf key3;     // tensor form, top three: every (object, tile)'s warp triples
     // sticky status word of the call's kernels (kStatusTimeout: a bounded pipeline wait of
     // the tensor form ran out; kStatusBadInput: non-finite or invalid inputs); zeroed when
     // allocated and after it is reported
     DevBuf status;
     void release() {
         DevBuf *b[] = {&objs, &offs, &perm, &rec, &tile_best, &counter, &keys, &optab, &partial,
-                       &status};
+                       &kbobj, &key3, &status};
         for (DevBuf *x : b) x->release();
     }
 };
@@ -119,6 +121,7 @@ struct Batch {
     std::vector<ObjInfo> objs;
     std::vector<uint32_t> perm;
     std::vector<uint64_t> offsets;
+    std::vector<uint32_t> kbobj;  // tensor form: object of each K-block (the table's rows)
 };
 
 int plan_batch(Batch &b, int sms, const MixedShape *shapes, uint32_t reanchor, int variant,
@@ -208,6 +211,11 @@ int plan_batch(Batch &b, int sms, const MixedShape *shapes, uint32_t reanchor, i
         }
         if (kb >= 0xffffffffull) return fail(LSGB_ERR_INVALID, "batch too long for the tensor form");
         b.total_kb = kb;
+        b.kbobj.resize(kb);
+        for (uint32_t o = 0; o < n_obj; ++o) {
+            const uint32_t nkb = (b.objs[o].n + kTensorKBlock - 1) / kTensorKBlock;
+            std::fill_n(b.kbobj.begin() + b.objs[o].kb0, nkb, o);
+        }
         // Fewer (object, tile) pairs than SMs: cut every object's K-blocks into slices so
         // that the units fill the SMs, each slice at least kMinSliceKB K-blocks long; a
         // finishing pass adds the slices' sums (one object of 3,555 observations and 1e5
@@ -267,6 +275,8 @@ int upload_tables(const Batch &b, Workspace &ws, cudaStream_t st) {
     if (mixed && b.shape.x2 == 3) LSGB_CUDA(ws.optab.ensure(tensor_optab_bytes(b.variant, b.total_kb)));
     if (mixed && b.shape.x2 == 3 && b.ksplit > 1)
         LSGB_CUDA(ws.partial.ensure(tensor_partial_bytes(b.variant) * b.units));
+    if (mixed && b.shape.x2 == 3 && b.ksplit <= 1 && b.top == 3 && b.want_best)
+        LSGB_CUDA(ws.key3.ensure(tensor_tile_key3_bytes((uint64_t)b.n_obj * b.n_tiles)));
     if (!ws.status.p) {
         LSGB_CUDA(ws.status.ensure(sizeof(uint32_t)));
         LSGB_CUDA(cudaMemsetAsync(ws.status.p, 0, sizeof(uint32_t), st));
@@ -277,6 +287,11 @@ int upload_tables(const Batch &b, Workspace &ws, cudaStream_t st) {
                               cudaMemcpyHostToDevice, st));
     LSGB_CUDA(cudaMemcpyAsync(ws.perm.p, b.perm.data(), sizeof(uint32_t) * b.n_obj,
                               cudaMemcpyHostToDevice, st));
+    if (mixed && b.shape.x2 == 3 && b.total_kb) {
+        LSGB_CUDA(ws.kbobj.ensure(sizeof(uint32_t) * b.total_kb));
+        LSGB_CUDA(cudaMemcpyAsync(ws.kbobj.p, b.kbobj.data(), sizeof(uint32_t) * b.total_kb,
+                                  cudaMemcpyHostToDevice, st));
+    }
     return LSGB_OK;
 }
 
@@ -365,6 +380,8 @@ int enqueue_batch(Batch &b, Workspace &ws, cudaStream_t st, cudaEvent_t ev0, cud
         a.top = b.top;
         a.wait_cycles = b.wait_cycles;
         a.ksplit = b.ksplit;
+        a.kb_obj = (const uint32_t *)ws.kbobj.p;
+        a.tile_key3 = (unsigned long long *)ws.key3.p;
         a.partial = b.ksplit > 1 ? (float *)ws.partial.p : nullptr;
         if (b.shape.x2 == 3) {
             LSGB_CUDA(launch_tensor_optab(b.variant, a, b.total_kb, st));

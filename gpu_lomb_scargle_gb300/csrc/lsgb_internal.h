@@ -106,6 +106,10 @@ struct MixedArgs {
                            // with slices, a unit's raw sums go to `partial` and a finishing
                            // pass forms the powers
     float *partial;        // tensor form with ksplit > 1: [units x tensor_partial_bytes]
+    const uint32_t *kb_obj;  // tensor form: the object of each K-block of the batch
+    unsigned long long *tile_key3;  // tensor form, top three, no slices: [n_obj x n_tiles x
+                                    // 4 x 3] the three best keys of each epilogue warp of
+                                    // each (object, tile), merged into best_key afterwards
 };
 
 
@@ -184,6 +188,7 @@ constexpr uint32_t kMinSliceKB = 16;
 size_t tensor_step_bytes(int variant);
 size_t tensor_optab_bytes(int variant, uint64_t total_kb);
 size_t tensor_partial_bytes(int variant);  // raw sums of one split unit
+size_t tensor_tile_key3_bytes(uint64_t pairs);  // top three: the warp triples of the pairs
 cudaError_t launch_tensor_optab(int variant, const MixedArgs &a, uint64_t total_kb, cudaStream_t st);
 // Compiled mixed shapes as (variant, F, threads, min CTAs, packed, unroll); returns the count.
 int mixed_shapes(int *out, int max_shapes);

@@ -888,7 +888,9 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             // split units store their raw sums for ksum_kernel instead of powers
             constexpr bool split = SPLIT;
             constexpr bool top3 = TOP3 && !SPLIT;
-            // the object's current third key: whatever is not above it is dropped here
+            static_assert(!top3 || kEpiPerQuarter == 1, "tile_key3 holds one triple per quarter");
+            // top three: the object's floor, a key no larger than its third best so far (the
+            // largest third key any warp has stored): whatever is not above it is dropped
             const unsigned long long g3 =
                 top3 ? *(volatile unsigned long long *)(a.best_key + 3ull * w.o + 2) : 0ull;
             Top3 t3;
@@ -983,14 +985,18 @@ __global__ void __launch_bounds__(kThreads, 1) tensor_kernel(MixedArgs a) {
             ring.push(rsum[0]);
             ring.push(rsum[1]);
             if constexpr (top3) {
-                // the warp's three best, then into the object's three slots; a warp none of
-                // whose lanes beat the seed has nothing to insert
-                if (__any_sync(0xffffffffu, t3.t0 > g3)) t3.warp_merge();
-                if (lane == 0 && t3.t0 > g3) {
-                    unsigned long long *slots = a.best_key + 3ull * w.o;
-                    top3_insert(slots, t3.t0);
-                    top3_insert(slots, t3.t1);
-                    top3_insert(slots, t3.t2);
+                // the warp's keys above the floor (at most three), stored for
+                // top3_merge_kernel; the warp's third key then raises the floor (a reduction
+                // without a return value: no round trip on this warp's path). A warp with
+                // nothing above the floor leaves its zeroed entries.
+                if (__any_sync(0xffffffffu, t3.t0 > g3)) {
+                    t3.warp_merge();
+                    if (lane < 3) {
+                        const unsigned long long key = lane == 0 ? t3.t0 : lane == 1 ? t3.t1 : t3.t2;
+                        a.tile_key3[(((uint64_t)w.o * a.n_tiles + w.tile) * 4u + eq) * 3u + lane] =
+                            key > g3 ? key : 0ull;
+                    }
+                    if (lane == 0 && t3.t2 > g3) atomicMax(a.best_key + 3ull * w.o + 2, t3.t2);
                 }
             } else if (!split && a.best_key) {
 #pragma unroll
@@ -1098,9 +1104,31 @@ __global__ void __launch_bounds__(256) ksum_kernel(MixedArgs a) {
     }
 }
 
-// The operand table: one CTA per (K-block, phase) builds the K-block's A matrices for
-// p < 128, split FP16 (re / im, hi / lo) in the layout the tensor kernel stages, and copies
-// them out coalesced; the phase-0 CTA also writes the K-block's steps array entries.
+// The top three of each object from its tiles' warp triples (tile_key3): one warp per
+// object offers the 12 n_tiles keys (distinct but for zeros) and merges its lanes' triples.
+// Every key of the object's top three is there: it is above every floor a warp saw (a floor
+// is some warp's third key, no larger than the object's third), and its own warp stored it.
+__global__ void __launch_bounds__(256) top3_merge_kernel(const unsigned long long *tile_key3,
+                                                         uint32_t n_obj, uint32_t n_tiles,
+                                                         unsigned long long *best_key) {
+    const uint32_t o = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t lane = threadIdx.x & 31u;
+    if (o >= n_obj) return;  // warp-uniform
+    const unsigned long long *src = tile_key3 + (uint64_t)o * n_tiles * 12u;
+    const uint32_t n = n_tiles * 12u;
+    Top3 t3;
+    for (uint32_t i = lane; i < n; i += 32u) {
+        const unsigned long long key = src[i];
+        if (key) t3.offer(key);
+    }
+    t3.warp_merge();
+    if (lane < 3) best_key[3ull * o + lane] = lane == 0 ? t3.t0 : lane == 1 ? t3.t1 : t3.t2;
+}
+
+// The operand table: one CTA per K-block builds its A matrices of both phases for p < 128,
+// split FP16 (re / im, hi / lo) in the layout the tensor kernel stages, from one sine /
+// cosine per (p, observation) (phase 1 by the double-angle formulas), copies them out
+// coalesced, and writes the K-block's steps array entries.
 //   standard:    phase 0 v0 tsc0 exp(i alpha), phase 1 exp(2i alpha); steps {b}
 //   generalized: phase 0 exp(i alpha),         phase 1 exp(2i alpha); steps {b, v0 tsc0,
 //                v1 tsc1} (the weights go on the right operand, built by the producers)
@@ -1109,23 +1137,17 @@ __global__ void __launch_bounds__(256) ksum_kernel(MixedArgs a) {
 template <bool GEN>
 __global__ void __launch_bounds__(256) agen_kernel(MixedArgs a, uint32_t total_kb) {
     using G = TGeo<GEN>;
-    __shared__ __align__(16) unsigned char ts[G::AKB];
-    const uint32_t kbg = blockIdx.x >> 1, ph = blockIdx.x & 1u;
+    __shared__ __align__(16) unsigned char ts[2 * G::AKB];  // [phase][A matrices]
+    const uint32_t kbg = blockIdx.x;
     if (kbg >= total_kb) return;
-    // the object of this K-block: the last o with kb0 <= kbg
-    uint32_t lo = 0, hi = a.n_obj;
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (a.objs[mid].kb0 <= kbg) lo = mid; else hi = mid;
-    }
-    const ObjInfo &ob = a.objs[lo];
+    const ObjInfo &ob = a.objs[a.kb_obj[kbg]];  // the object of this K-block
     const uint32_t kb = kbg - ob.kb0;
     const uint32_t cnt = min((uint32_t)kTK, ob.n - kb * kTK);
     const ObsRec *rec = static_cast<const ObsRec *>(a.rec) + ob.row0 + (uint64_t)kb * kTK;
     const float sc0 = ob.tsc0, sc1 = ob.tsc1;
     for (uint32_t e = threadIdx.x; e < (uint32_t)kTP * (kTK / 4); e += blockDim.x) {
         const uint32_t p = e >> 2, j0 = 4u * (e & 3u);
-        float x[2][4];  // [re / im][observation]
+        float x[2][2][4];  // [phase][re / im][observation]
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const uint32_t j = j0 + (uint32_t)q;
@@ -1135,27 +1157,28 @@ __global__ void __launch_bounds__(256) agen_kernel(MixedArgs a, uint32_t total_k
             float sn, cs;
             turn_sincos(t32, sn, cs);
             const float mk = j < cnt ? 1.0f : 0.0f;
-            if (ph == 0) {
-                const float v = (GEN ? 1.0f : r.v0 * sc0) * mk;
-                x[0][q] = v * cs;
-                x[1][q] = v * sn;
-            } else {
-                x[0][q] = mk * fmaf(cs, cs, -sn * sn);
-                x[1][q] = mk * (2.0f * cs * sn);
+            const float v = (GEN ? 1.0f : r.v0 * sc0) * mk;
+            x[0][0][q] = v * cs;
+            x[0][1][q] = v * sn;
+            x[1][0][q] = mk * fmaf(cs, cs, -sn * sn);
+            x[1][1][q] = mk * (2.0f * cs * sn);
+        }
+#pragma unroll
+        for (int ph = 0; ph < 2; ++ph)
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                float h4[4], l4[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) vsplit(x[ph][c][q], h4[q], l4[q]);
+                unsigned char *base = ts + (uint32_t)ph * G::AKB +
+                                      2u * (uint32_t)c * G::A_BYTES + kmaj_off(p, j0);
+                *reinterpret_cast<uint2 *>(base) =
+                    make_uint2(pack_h2(h4[0], h4[1]), pack_h2(h4[2], h4[3]));
+                *reinterpret_cast<uint2 *>(base + G::A_BYTES) =
+                    make_uint2(pack_h2(l4[0], l4[1]), pack_h2(l4[2], l4[3]));
             }
-        }
-#pragma unroll
-        for (int c = 0; c < 2; ++c) {
-            float h4[4], l4[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) vsplit(x[c][q], h4[q], l4[q]);
-            unsigned char *base = ts + 2u * (uint32_t)c * G::A_BYTES + kmaj_off(p, j0);
-            *reinterpret_cast<uint2 *>(base) = make_uint2(pack_h2(h4[0], h4[1]), pack_h2(h4[2], h4[3]));
-            *reinterpret_cast<uint2 *>(base + G::A_BYTES) =
-                make_uint2(pack_h2(l4[0], l4[1]), pack_h2(l4[2], l4[3]));
-        }
     }
-    if (ph == 0 && threadIdx.x < (uint32_t)kTK) {
+    if (threadIdx.x < (uint32_t)kTK) {
         const uint32_t j = threadIdx.x;
         const bool in = j < cnt;
         const uint32_t b_lo = in ? rec[j].b_lo : 0u, b_hi = in ? rec[j].b_hi : 0u;
@@ -1169,10 +1192,15 @@ __global__ void __launch_bounds__(256) agen_kernel(MixedArgs a, uint32_t total_k
             *reinterpret_cast<uint2 *>(dst) = make_uint2(b_lo, b_hi);
     }
     __syncthreads();
-    uint4 *dst = reinterpret_cast<uint4 *>(static_cast<unsigned char *>(const_cast<void *>(a.optab)) +
-                                           ((uint64_t)ph * total_kb + kbg) * G::AKB);
+    constexpr uint32_t N16 = (uint32_t)G::AKB / 16u;  // 16-byte words per phase
     const uint4 *src = reinterpret_cast<const uint4 *>(ts);
-    for (uint32_t i = threadIdx.x; i < (uint32_t)G::AKB / 16u; i += blockDim.x) dst[i] = src[i];
+    unsigned char *tab = static_cast<unsigned char *>(const_cast<void *>(a.optab));
+    uint4 *dst0 = reinterpret_cast<uint4 *>(tab + (uint64_t)kbg * G::AKB);
+    uint4 *dst1 = reinterpret_cast<uint4 *>(tab + ((uint64_t)total_kb + kbg) * G::AKB);
+    for (uint32_t i = threadIdx.x; i < N16; i += blockDim.x) {
+        dst0[i] = src[i];
+        dst1[i] = src[N16 + i];
+    }
 }
 
 template <bool GEN>
@@ -1211,7 +1239,7 @@ size_t tensor_optab_bytes(int variant, uint64_t total_kb) {
 
 cudaError_t launch_tensor_optab(int variant, const MixedArgs &a, uint64_t total_kb, cudaStream_t st) {
     if (total_kb == 0) return cudaSuccess;
-    const uint64_t blocks = total_kb * 2u;
+    const uint64_t blocks = total_kb;
     if (blocks > 0x7fffffffull) return cudaErrorInvalidValue;
     if (variant == 0)
         agen_kernel<false><<<(unsigned)blocks, 256, 0, st>>>(a, (uint32_t)total_kb);
@@ -1222,11 +1250,24 @@ cudaError_t launch_tensor_optab(int variant, const MixedArgs &a, uint64_t total_
 
 cudaError_t launch_tensor(int variant, int dtype, const MixedArgs &a, int grid, cudaStream_t st) {
     cudaError_t e;
+    if (a.ksplit <= 1u && a.top == 3u && a.best_key) {
+        e = cudaMemsetAsync(a.tile_key3, 0, tensor_tile_key3_bytes((uint64_t)a.n_obj * a.n_tiles), st);
+        if (e != cudaSuccess) return e;
+    }
     if (variant == 0)
         e = dtype == 0 ? launch_t<false, float>(a, grid, st) : launch_t<false, double>(a, grid, st);
     else
         e = dtype == 0 ? launch_t<true, float>(a, grid, st) : launch_t<true, double>(a, grid, st);
-    if (e != cudaSuccess || a.ksplit <= 1u) return e;
+    if (e != cudaSuccess) return e;
+    if (a.ksplit <= 1u) {
+        if (a.top != 3u || !a.best_key) return cudaSuccess;
+        // top three: merge the tiles' warp triples
+        const uint64_t blocks = ((uint64_t)a.n_obj * 32u + 255u) / 256u;
+        if (blocks > 0x7fffffffull) return cudaErrorInvalidValue;
+        top3_merge_kernel<<<(unsigned)blocks, 256, 0, st>>>(a.tile_key3, a.n_obj, a.n_tiles,
+                                                             a.best_key);
+        return cudaGetLastError();
+    }
     // split units: the finishing pass over every (object, tile) pair
     const uint64_t blocks = (uint64_t)a.n_obj * a.n_tiles * (tensor_tile_freqs(variant) / kKsumFreqs);
     if (blocks > 0x7fffffffull) return cudaErrorInvalidValue;
@@ -1239,6 +1280,8 @@ cudaError_t launch_tensor(int variant, int dtype, const MixedArgs &a, int grid, 
     }
     return cudaGetLastError();
 }
+
+size_t tensor_tile_key3_bytes(uint64_t pairs) { return sizeof(unsigned long long) * 12u * pairs; }
 
 size_t tensor_partial_bytes(int variant) {
     return sizeof(float) * (variant ? 6u * (size_t)TGeo<true>::TILE : 4u * (size_t)TGeo<false>::TILE);
