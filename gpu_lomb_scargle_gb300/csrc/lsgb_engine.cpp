@@ -228,6 +228,17 @@ int plan_batch(Batch &b, int sms, const MixedShape *shapes, uint32_t reanchor, i
             b.ksplit = (uint32_t)std::max<uint64_t>(1, std::min(by_sms, by_len));
         }
         b.units *= b.ksplit;
+        // The tensor kernel walks its units statically (CTA c takes units c, c + grid, ...),
+        // so the order is not for load balance but for overlap: largest and smallest objects
+        // alternate, so that a CTA's short units (whose power pass outlasts their MMAs) fall
+        // between long ones and the TMEM slots absorb them (0.4% at 999 objects).
+        std::vector<uint32_t> alt;
+        alt.reserve(n_obj);
+        for (size_t lo = 0, hi = n_obj; lo < hi;) {
+            alt.push_back(b.perm[lo++]);
+            if (lo < hi) alt.push_back(b.perm[--hi]);
+        }
+        b.perm.swap(alt);
     } else if (mixed) {
         // Shared memory per CTA: at most what keeps the CTAs per SM that the shape's
         // register budget allows resident (less the per-CTA reservation and the static
