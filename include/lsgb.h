@@ -183,8 +183,7 @@ LSGB_API int lsgb_set_tuning(lsgb_engine *eng, int variant, int freqs_per_thread
  * tile) units, a tile being 3072 frequencies for LSGB_STANDARD and 2048 for
  * LSGB_GENERALIZED; larger calls return LSGB_ERR_INVALID with the limit in
  * lsgb_last_error(). The first call on each device looks up the scratch array's
- * device address on that device (make that first call before any stream capture).
- * All calls share the one array and leave its contents behind, so calls whose GPU
+ * device address on that device. All calls share the one array and leave its contents behind, so calls whose GPU
  * work overlaps (different streams or host threads without ordering) race; order
  * them. Host set-up is serialized internally and waits for the stream's earlier
  * work before launching. */
