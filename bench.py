@@ -134,8 +134,8 @@ class ClockSampler:
 
 
 def tensor_peak_tflops():
-    """(peak TFLOP/s, source) of dense bf16/FP16 MMA: the measured burst figure,
-    else the fallback."""
+    """(peak TFLOP/s, source) of dense bf16/FP16 MMA: the burst figure measured on this
+    GPU model (MEASURED_PEAKS.json), else the fallback."""
     try:
         d = json.loads(MEASURED_PEAKS.read_text())
         return float(d["bf16_tflops"]), "MEASURED_PEAKS.json bf16_tflops (burst), of measured"
