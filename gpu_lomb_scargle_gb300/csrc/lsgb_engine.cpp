@@ -807,10 +807,16 @@ static int periodogram_host(lsgb_engine *eng, int variant, int precision, int dt
             LSGB_CUDA(eng->ws.keys.ensure(sizeof(unsigned long long) * n_obj * top));
             if (precision == LSGB_MIXED)
                 LSGB_CUDA(eng->ws.rec.ensure(mixed_global_rec_bytes(eng->shape[variant]) * rows));
-            if (precision == LSGB_MIXED && eng->shape[variant].x2 == 3)
-                LSGB_CUDA(eng->ws.optab.ensure(
-                    tensor_optab_bytes(variant, rows / kTensorKBlock + n_obj)));
-            else if (best_idx || best_power)
+            if (precision == LSGB_MIXED && eng->shape[variant].x2 == 3) {
+                const uint64_t kb = rows / kTensorKBlock + n_obj;  // K-blocks, at most
+                LSGB_CUDA(eng->ws.optab.ensure(tensor_optab_bytes(variant, kb)));
+                LSGB_CUDA(eng->ws.kbobj.ensure(sizeof(uint32_t) * kb));
+                LSGB_CUDA(eng->ws.partial.ensure(tensor_partial_bytes(variant) * (size_t)eng->sms));
+                if (top == 3 && (best_idx || best_power))
+                    LSGB_CUDA(eng->ws.key3.ensure(tensor_tile_key3_bytes(
+                        (uint64_t)n_obj * ((n_freq + tensor_tile_freqs(variant) - 1) /
+                                           tensor_tile_freqs(variant)))));
+            } else if (best_idx || best_power)
                 LSGB_CUDA(eng->ws.tile_best.ensure(sizeof(TileBest) * max_tiles * n_obj * top));
         }
         std::vector<cudaEvent_t> ev(cut.size() - 1, nullptr);
