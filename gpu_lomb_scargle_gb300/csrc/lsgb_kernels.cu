@@ -143,33 +143,31 @@ __global__ void stats_kernel(int variant, int mixed, int dtype, int normalize, c
     // generalized variant a non-finite or non-positive dmag (weight 1/dmag^2). The
     // reference computes NaN or infinite powers from them; here the call reports them
     // (status bit 1, kStatusBadInput) and its results for that object mean nothing.
-    if (status) {
-        bool bad = false;
-        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-            bad |= !isfinite(load_in(dtype, t, r0 + i)) || !isfinite(load_in(dtype, y, r0 + i));
-            if (variant) {
-                const double e = load_in(dtype, dy, r0 + i);
-                bad |= !(isfinite(e) && e > 0.0);
-            }
-        }
-        if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(status, kStatusBadInput);
-    }
+    // The loops below are unrolled so that a thread's loads are in flight together (one
+    // object is one CTA, so its passes are latency-bound); each thread still accumulates its
+    // rows i = tid, tid + blockDim, ... in order, so the sums do not change.
     if (variant == 0) {
-        double s = 0.0;
-        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) s += load_in(dtype, y, r0 + i);
+        // pass 1: the input check, the sum and (mixed form) the largest |y| as a float
+        bool bad = false;
+        double s = 0.0, ym = 0.0;
+#pragma unroll 4
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+            const double yi = load_in(dtype, y, r0 + i);
+            if (status) bad |= !isfinite(load_in(dtype, t, r0 + i)) || !isfinite(yi);
+            s += yi;
+            ym = fmax(ym, fabs((double)(float)yi));
+        }
+        if (status && __syncthreads_or(bad) && threadIdx.x == 0) atomicOr(status, kStatusBadInput);
         const double mean = block_sum(s, s_red) / (n * 1.0);
+        ym = mixed ? block_max(ym, s_red) : 0.0;
+        // pass 2: the centred sum of squares
         double s2 = 0.0;
+#pragma unroll 4
         for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
             const double d = load_in(dtype, y, r0 + i) - mean;
             s2 += d * d;
         }
         s2 = block_sum(s2, s_red);
-        double ym = 0.0;
-        if (mixed) {
-            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
-                ym = fmax(ym, fabs((double)(float)load_in(dtype, y, r0 + i)));
-            ym = block_max(ym, s_red);
-        }
         if (threadIdx.x == 0) {
             const double sigma = sqrt(s2 / (n * 1.0));
             ob.norm = normalize ? 2.0 / (n * (sigma * sigma)) : 1.0;
@@ -179,6 +177,22 @@ __global__ void stats_kernel(int variant, int mixed, int dtype, int normalize, c
         }
         return;
     }
+    // generalized: pass 1, the input check and (mixed form) the weight sums
+    bool bad = false;
+    double w_s = 0.0, wy_s = 0.0;
+#pragma unroll 4
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const double e = load_in(dtype, dy, r0 + i), yi = load_in(dtype, y, r0 + i);
+        if (status)
+            bad |= !isfinite(load_in(dtype, t, r0 + i)) || !isfinite(yi) || !(isfinite(e) && e > 0.0);
+        if (mixed) {
+            double w = 1.0 / e;
+            w = w * w;
+            w_s += w;
+            wy_s += w * yi;
+        }
+    }
+    if (status && __syncthreads_or(bad) && threadIdx.x == 0) atomicOr(status, kStatusBadInput);
     if (!mixed) {
         if (threadIdx.x == 0) {
             ob.norm = 1.0;
@@ -186,16 +200,10 @@ __global__ void stats_kernel(int variant, int mixed, int dtype, int normalize, c
         }
         return;
     }
-    double w_s = 0.0, wy_s = 0.0;
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-        double w = 1.0 / load_in(dtype, dy, r0 + i);
-        w = w * w;
-        w_s += w;
-        wy_s += w * load_in(dtype, y, r0 + i);
-    }
     const double W = block_sum(w_s, s_red);
     const double ym = block_sum(wy_s, s_red) / W;
     double wf_s = 0.0, yf_s = 0.0, yy_s = 0.0, m0 = 0.0, m1 = 0.0;
+#pragma unroll 4
     for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
         double w = 1.0 / load_in(dtype, dy, r0 + i);
         w = w * w;
