@@ -368,7 +368,8 @@ int enqueue_batch(Batch &b, Workspace &ws, cudaStream_t st, cudaEvent_t ev0, cud
         two_prod(b.df, kInv2PiHi, kInv2PiLo, g.df_hi, g.df_lo);
         LSGB_CUDA(launch_records(b.variant, b.dtype, b.t, b.y, b.dy, (const uint64_t *)ws.offs.p,
                                  b.n_obj, d_objs, b.rows, g, ws.rec.p,
-                                 b.shape.x2 == 2 ? (uint32_t)b.shape.nt : 0u, st));
+                                 b.shape.x2 == 2 ? (uint32_t)b.shape.nt : 0u, st,
+                                 /*rotation=*/b.shape.x2 != 3));
         ++kernels;
         MixedArgs a{};
         a.rec = ws.rec.p;

@@ -12,7 +12,7 @@ namespace lsgb {
 //   f0 = fmin / 2pi and dfturn = df / 2pi, so the phase of grid point k is
 //   a + k*b (mod 2^64), exact to ~(1+k) * 2^-64 turns;
 //   cd, sd = cos, sin(2 pi s b): the rotation by s grid points (s = 1 for the
-//   recurrence loops; the tensor form does not use them);
+//   recurrence loops; the tensor form does not use them, and its records leave them 0);
 //   standard:    v0 = y,          v1 = 0
 //   generalized: v0 = w / W,      v1 = (w / W) * (y - ybar_w),   w = 1/dy^2.
 struct __align__(16) ObsRec {
@@ -160,7 +160,7 @@ cudaError_t launch_stats(int variant, int mixed, int dtype, int normalize, const
 cudaError_t launch_records(int variant, int dtype, const void *t, const void *y, const void *dy,
                            const uint64_t *offsets, uint32_t n_obj, const ObjInfo *objs,
                            uint64_t rows, GridTurns g, void *rec, uint32_t so_stride,
-                           cudaStream_t st);
+                           cudaStream_t st, bool rotation = true);
 // Mixed kernel: returns cudaErrorInvalidValue when (variant, dtype, shape) is not compiled.
 cudaError_t launch_mixed(int variant, int dtype, MixedShape shape, const MixedArgs &a,
                          int grid, size_t smem, cudaStream_t st);

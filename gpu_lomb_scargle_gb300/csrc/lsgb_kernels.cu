@@ -241,7 +241,7 @@ __global__ void stats_kernel(int variant, int mixed, int dtype, int normalize, c
 __global__ void records_kernel(int variant, int dtype, const void *t, const void *y,
                                const void *dy, const uint64_t *offsets, uint32_t n_obj,
                                const ObjInfo *objs, uint64_t rows, GridTurns g, void *rec,
-                               uint32_t so_stride) {
+                               uint32_t so_stride, int rotation) {
     for (uint64_t row = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; row < rows;
          row += (uint64_t)gridDim.x * blockDim.x) {
         const double td = load_in(dtype, t, row);
@@ -250,8 +250,8 @@ __global__ void records_kernel(int variant, int dtype, const void *t, const void
         // the step of the recurrence: one grid point, or so_stride of them (exact in the
         // fixed-point turns; the signed reading puts the angle in [-pi, pi))
         const uint64_t bs = b * (uint64_t)(so_stride ? so_stride : 1u);
-        double sd, cd;
-        sincos((double)(long long)bs * kTwoPiOver2p64, &sd, &cd);
+        double sd = 0.0, cd = 0.0;  // (an FP64 sine/cosine: skipped for the tensor form)
+        if (rotation) sincos((double)(long long)bs * kTwoPiOver2p64, &sd, &cd);
         ObsRec r;
         r.a_lo = (uint32_t)a;
         r.a_hi = (uint32_t)(a >> 32);
@@ -1073,12 +1073,12 @@ cudaError_t launch_stats(int variant, int mixed, int dtype, int normalize, const
 cudaError_t launch_records(int variant, int dtype, const void *t, const void *y, const void *dy,
                            const uint64_t *offsets, uint32_t n_obj, const ObjInfo *objs,
                            uint64_t rows, GridTurns g, void *rec, uint32_t so_stride,
-                           cudaStream_t st) {
+                           cudaStream_t st, bool rotation) {
     if (rows == 0) return cudaSuccess;
     const uint64_t blocks64 = (rows + 255) / 256;
     const int blocks = (int)(blocks64 < 65535ull * 16 ? blocks64 : 65535ull * 16);
     records_kernel<<<blocks, 256, 0, st>>>(variant, dtype, t, y, dy, offsets, n_obj, objs, rows, g,
-                                           rec, so_stride);
+                                           rec, so_stride, rotation || so_stride ? 1 : 0);
     return cudaGetLastError();
 }
 

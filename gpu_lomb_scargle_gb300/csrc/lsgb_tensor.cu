@@ -1127,17 +1127,18 @@ __global__ void __launch_bounds__(256) top3_merge_kernel(const unsigned long lon
 
 // The operand table: one CTA per K-block builds its A matrices of both phases for p < 128,
 // split FP16 (re / im, hi / lo) in the layout the tensor kernel stages, from one sine /
-// cosine per (p, observation) (phase 1 by the double-angle formulas), copies them out
-// coalesced, and writes the K-block's steps array entries.
+// cosine per (p, observation) (phase 1 by the double-angle formulas), and writes the
+// K-block's steps array entries.
 //   standard:    phase 0 v0 tsc0 exp(i alpha), phase 1 exp(2i alpha); steps {b}
 //   generalized: phase 0 exp(i alpha),         phase 1 exp(2i alpha); steps {b, v0 tsc0,
 //                v1 tsc1} (the weights go on the right operand, built by the producers)
 // with alpha = a + p b in 64-bit fixed point. Observations past the object's end get zero
-// A entries (and zero steps and weights), so they add nothing to any product.
+// A entries (and zero steps and weights), so they add nothing to any product. A thread's
+// four observations of one row p are 8 contiguous bytes of a core matrix, and a warp's
+// eight rows two whole 128-byte lines, so the entries go straight to global memory.
 template <bool GEN>
 __global__ void __launch_bounds__(256) agen_kernel(MixedArgs a, uint32_t total_kb) {
     using G = TGeo<GEN>;
-    __shared__ __align__(16) unsigned char ts[2 * G::AKB];  // [phase][A matrices]
     const uint32_t kbg = blockIdx.x;
     if (kbg >= total_kb) return;
     const ObjInfo &ob = a.objs[a.kb_obj[kbg]];  // the object of this K-block
@@ -1145,6 +1146,9 @@ __global__ void __launch_bounds__(256) agen_kernel(MixedArgs a, uint32_t total_k
     const uint32_t cnt = min((uint32_t)kTK, ob.n - kb * kTK);
     const ObsRec *rec = static_cast<const ObsRec *>(a.rec) + ob.row0 + (uint64_t)kb * kTK;
     const float sc0 = ob.tsc0, sc1 = ob.tsc1;
+    unsigned char *tab = static_cast<unsigned char *>(const_cast<void *>(a.optab));
+    unsigned char *const dst[2] = {tab + (uint64_t)kbg * G::AKB,
+                                   tab + ((uint64_t)total_kb + kbg) * G::AKB};
     for (uint32_t e = threadIdx.x; e < (uint32_t)kTP * (kTK / 4); e += blockDim.x) {
         const uint32_t p = e >> 2, j0 = 4u * (e & 3u);
         float x[2][2][4];  // [phase][re / im][observation]
@@ -1170,8 +1174,7 @@ __global__ void __launch_bounds__(256) agen_kernel(MixedArgs a, uint32_t total_k
                 float h4[4], l4[4];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) vsplit(x[ph][c][q], h4[q], l4[q]);
-                unsigned char *base = ts + (uint32_t)ph * G::AKB +
-                                      2u * (uint32_t)c * G::A_BYTES + kmaj_off(p, j0);
+                unsigned char *base = dst[ph] + 2u * (uint32_t)c * G::A_BYTES + kmaj_off(p, j0);
                 *reinterpret_cast<uint2 *>(base) =
                     make_uint2(pack_h2(h4[0], h4[1]), pack_h2(h4[2], h4[3]));
                 *reinterpret_cast<uint2 *>(base + G::A_BYTES) =
@@ -1182,24 +1185,14 @@ __global__ void __launch_bounds__(256) agen_kernel(MixedArgs a, uint32_t total_k
         const uint32_t j = threadIdx.x;
         const bool in = j < cnt;
         const uint32_t b_lo = in ? rec[j].b_lo : 0u, b_hi = in ? rec[j].b_hi : 0u;
-        unsigned char *dst = static_cast<unsigned char *>(const_cast<void *>(a.steps)) +
-                             ((uint64_t)kbg * kTK + j) * (uint32_t)G::SB;
+        unsigned char *sdst = static_cast<unsigned char *>(const_cast<void *>(a.steps)) +
+                              ((uint64_t)kbg * kTK + j) * (uint32_t)G::SB;
         if (GEN)
-            *reinterpret_cast<uint4 *>(dst) =
+            *reinterpret_cast<uint4 *>(sdst) =
                 make_uint4(b_lo, b_hi, __float_as_uint(in ? rec[j].v0 * sc0 : 0.0f),
                            __float_as_uint(in ? rec[j].v1 * sc1 : 0.0f));
         else
-            *reinterpret_cast<uint2 *>(dst) = make_uint2(b_lo, b_hi);
-    }
-    __syncthreads();
-    constexpr uint32_t N16 = (uint32_t)G::AKB / 16u;  // 16-byte words per phase
-    const uint4 *src = reinterpret_cast<const uint4 *>(ts);
-    unsigned char *tab = static_cast<unsigned char *>(const_cast<void *>(a.optab));
-    uint4 *dst0 = reinterpret_cast<uint4 *>(tab + (uint64_t)kbg * G::AKB);
-    uint4 *dst1 = reinterpret_cast<uint4 *>(tab + ((uint64_t)total_kb + kbg) * G::AKB);
-    for (uint32_t i = threadIdx.x; i < N16; i += blockDim.x) {
-        dst0[i] = src[i];
-        dst1[i] = src[N16 + i];
+            *reinterpret_cast<uint2 *>(sdst) = make_uint2(b_lo, b_hi);
     }
 }
 
