@@ -273,12 +273,16 @@ void dispatcher(lsgb_server *s) {
             if (!busy) break;
         }
         if (!launched) {
-            std::unique_lock<std::mutex> lk(s->mu);
-            if (any_busy)
-                s->cv.wait_for(lk, std::chrono::microseconds(20));
-            else
+            if (any_busy) {
+                // a batch is on the GPU: poll its event again at once, so that its completion
+                // time is taken when it completes (a timed sleep here overshoots by tens of
+                // microseconds, the size of a small batch's whole latency)
+                std::this_thread::yield();
+            } else {
+                std::unique_lock<std::mutex> lk(s->mu);
                 s->cv.wait_for(lk, std::chrono::milliseconds(2),
                                [&] { return !s->pending.empty() || s->stop.load(); });
+            }
         }
     }
 }
