@@ -356,11 +356,11 @@ int enqueue_batch(Batch &b, Workspace &ws, cudaStream_t st, cudaEvent_t ev0, cud
     const bool mixed = b.precision == LSGB_MIXED;
     ObjInfo *d_objs = (ObjInfo *)ws.objs.p;
     uint32_t kernels = 0;
-    LSGB_CUDA(cudaMemsetAsync(ws.counter.p, 0, sizeof(uint32_t), st));
-    if (b.want_best && mixed)
-        LSGB_CUDA(cudaMemsetAsync(ws.keys.p, 0, sizeof(unsigned long long) * b.n_obj * b.top, st));
+    // the statistics kernel also zeroes the queue counter and the best keys
     LSGB_CUDA(launch_stats(b.variant, mixed ? 1 : 0, b.dtype, b.normalize, b.t, b.y, b.dy, d_objs,
-                           b.n_obj, (uint32_t *)ws.status.p, st));
+                           b.n_obj, (uint32_t *)ws.status.p, st,
+                           b.want_best && mixed ? (unsigned long long *)ws.keys.p : nullptr, b.top,
+                           (uint32_t *)ws.counter.p));
     ++kernels;
     if (mixed) {
         GridTurns g;

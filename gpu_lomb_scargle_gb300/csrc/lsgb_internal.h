@@ -150,9 +150,12 @@ constexpr uint32_t kStatusTimeout = 1u;   // a bounded pipeline wait of the tens
 constexpr uint32_t kStatusBadInput = 2u;  // a non-finite t / y, or a non-finite or non-positive
                                           // dy (generalized variant)
 // Per-object statistics; when status is non-null it also checks the inputs (kStatusBadInput).
+// Also zeroes, when given, each object's `top` best keys and the work-queue counter (the
+// kernels that use them run after it), in place of two memsets.
 cudaError_t launch_stats(int variant, int mixed, int dtype, int normalize, const void *t,
                          const void *y, const void *dy, ObjInfo *objs, uint32_t n_obj,
-                         uint32_t *status, cudaStream_t st);
+                         uint32_t *status, cudaStream_t st, unsigned long long *keys = nullptr,
+                         uint32_t top = 0, uint32_t *counter = nullptr);
 // so_stride 0: ObsRec records whose (cd, sd) step is one grid point (the rotation loops;
 // the tensor form reads only a, b, v0, v1); > 0: SoRec records for a
 // second-order shape whose CTA has so_stride threads. `rec` holds rows x 32 or rows x 96

@@ -134,8 +134,11 @@ __device__ float pow2_scale(double m) {
 }
 
 __global__ void stats_kernel(int variant, int mixed, int dtype, int normalize, const void *t,
-                             const void *y, const void *dy, ObjInfo *objs, uint32_t *status) {
+                             const void *y, const void *dy, ObjInfo *objs, uint32_t *status,
+                             unsigned long long *keys, uint32_t top, uint32_t *counter) {
     __shared__ double s_red[32];
+    if (keys && threadIdx.x < top) keys[(uint64_t)blockIdx.x * top + threadIdx.x] = 0ull;
+    if (counter && blockIdx.x == 0 && threadIdx.x == 0) *counter = 0u;
     ObjInfo &ob = objs[blockIdx.x];
     const uint64_t r0 = ob.row0;
     const uint32_t n = ob.n;
@@ -1064,9 +1067,11 @@ cudaError_t occ_mixed_t(int dtype, size_t smem, int *blocks) {
 
 cudaError_t launch_stats(int variant, int mixed, int dtype, int normalize, const void *t,
                          const void *y, const void *dy, ObjInfo *objs, uint32_t n_obj,
-                         uint32_t *status, cudaStream_t st) {
+                         uint32_t *status, cudaStream_t st, unsigned long long *keys,
+                         uint32_t top, uint32_t *counter) {
     if (n_obj == 0) return cudaSuccess;
-    stats_kernel<<<n_obj, 256, 0, st>>>(variant, mixed, dtype, normalize, t, y, dy, objs, status);
+    stats_kernel<<<n_obj, 256, 0, st>>>(variant, mixed, dtype, normalize, t, y, dy, objs, status,
+                                        keys, top, counter);
     return cudaGetLastError();
 }
 
