@@ -200,7 +200,10 @@ LSGB_API int lsgb_periodogram_noalloc(int variant, int dtype, const void *t, con
  * while the device bytes of all in-flight batches stay under hbm_budget_bytes (a
  * single object larger than the budget runs alone), and launches it on the slot's
  * own stream and engine, so up to `slots` batches overlap on the GPU. Every object
- * gets the best frequency index and power of its periodogram over one shared grid. */
+ * gets the best frequency index and power of its periodogram over one shared grid.
+ * While a batch is on the GPU the dispatcher polls its completion without sleeping
+ * (one host core busy), so that results are published as soon as they are ready; with
+ * nothing in flight it blocks until an object is submitted. */
 typedef struct lsgb_server lsgb_server;
 
 LSGB_API int lsgb_server_create(int device, int variant, int precision, double fmin, double df,
