@@ -461,7 +461,25 @@ struct lsgb_engine {
     bool ev_valid = false;
     uint32_t reanchor = 0;  // mixed form: 0 = anchor at each thread's frequency run
     long long wait_cycles = 0;  // lsgb_set_wait_limit
+    uint32_t *h_status = nullptr;  // pinned: the status word, copied back with a call's results
 };
+
+// Ends a host-buffer call whose results are queued for copy on st: the status word is
+// copied back on the same stream, so one synchronization brings both (a separate
+// synchronous read would cost another round trip); then it is reported and cleared.
+static int finish_host_call(lsgb_engine *eng, cudaStream_t st) {
+    if (!eng->ws.status.p) {
+        LSGB_CUDA(cudaStreamSynchronize(st));
+        return LSGB_OK;
+    }
+    LSGB_CUDA(cudaMemcpyAsync(eng->h_status, eng->ws.status.p, sizeof(uint32_t),
+                              cudaMemcpyDeviceToHost, st));
+    LSGB_CUDA(cudaStreamSynchronize(st));
+    const uint32_t v = *eng->h_status;
+    if (v == 0) return LSGB_OK;
+    LSGB_CUDA(cudaMemset(eng->ws.status.p, 0, sizeof(uint32_t)));
+    return status_code(v);
+}
 
 // A batch whose device work is captured once in a CUDA graph and replayed.
 struct lsgb_plan {
@@ -499,6 +517,7 @@ LSGB_API int lsgb_engine_create(int device, lsgb_engine **out) {
     if (e2 == cudaSuccess) e2 = cudaStreamCreateWithFlags(&eng->d2h, cudaStreamNonBlocking);
     if (e2 == cudaSuccess) e2 = cudaEventCreate(&eng->ev_main0);
     if (e2 == cudaSuccess) e2 = cudaEventCreate(&eng->ev_main1);
+    if (e2 == cudaSuccess) e2 = cudaHostAlloc((void **)&eng->h_status, sizeof(uint32_t), 0);
     if (e2 != cudaSuccess) {
         delete eng;
         return fail(LSGB_ERR_CUDA, "engine set-up failed: %s", cudaGetErrorString(e2));
@@ -518,6 +537,7 @@ LSGB_API void lsgb_engine_destroy(lsgb_engine *eng) {
     if (eng->d2h) cudaStreamDestroy(eng->d2h);
     if (eng->ev_main0) cudaEventDestroy(eng->ev_main0);
     if (eng->ev_main1) cudaEventDestroy(eng->ev_main1);
+    if (eng->h_status) cudaFreeHost(eng->h_status);
     delete eng;
 }
 
@@ -858,8 +878,7 @@ static int periodogram_host(lsgb_engine *eng, int variant, int precision, int dt
                                       cudaMemcpyDeviceToHost, st));
         if (d_p)
             LSGB_CUDA(cudaMemcpyAsync(best_power, d_p, es * n_obj * top, cudaMemcpyDeviceToHost, st));
-        LSGB_CUDA(cudaStreamSynchronize(st));
-        return check_status(eng->ws);
+        return finish_host_call(eng, st);
     }
     int rc = periodogram_device(eng, variant, precision, dtype, eng->in_t.p, eng->in_y.p, d_dy,
                                 offsets, n_obj, fmin, df, n_freq, normalize, d_pg, d_idx, d_p,
@@ -880,8 +899,7 @@ static int periodogram_host(lsgb_engine *eng, int variant, int precision, int dt
         LSGB_CUDA(cudaMemcpyAsync(best_idx, d_idx, sizeof(uint32_t) * n_obj * top,
                                   cudaMemcpyDeviceToHost, st));
     if (d_p) LSGB_CUDA(cudaMemcpyAsync(best_power, d_p, es * n_obj * top, cudaMemcpyDeviceToHost, st));
-    LSGB_CUDA(cudaStreamSynchronize(st));
-    return check_status(eng->ws);
+    return finish_host_call(eng, st);
 }
 
 LSGB_API int lsgb_periodogram_host(lsgb_engine *eng, int variant, int precision, int dtype,
