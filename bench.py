@@ -376,6 +376,35 @@ def main():
     value = w.pairs * world / (ms / 1e3)
     best_idx = bi.cpu().numpy()
 
+    # e2e through the host-buffer C ABI with pinned inputs, on every rank at once (a barrier
+    # before, the slowest rank's time after)
+    th = torch.from_numpy(w.t).pin_memory().numpy()
+    yh = torch.from_numpy(w.y).pin_memory().numpy()
+    oi = torch.empty(w.n_obj, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+    op = torch.empty(w.n_obj, dtype=torch.float64).pin_memory().numpy()
+    offs = np.ascontiguousarray(w.offsets, np.uint64)  # the caller's row offsets, once
+    for _ in range(2):
+        eng.run_host(0, "mixed", th, yh, None, offs, w.fmin, w.df, w.n_freq, True,
+                     out_idx=oi, out_power=op)
+    if world > 1:
+        torch.distributed.barrier()
+    e2e_t = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        eng.run_host(0, "mixed", th, yh, None, offs, w.fmin, w.df, w.n_freq, True,
+                     out_idx=oi, out_power=op)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = float(np.mean(e2e_t))
+    if world > 1:
+        from gpu_lomb_scargle_gb300 import shard
+        e2e_s = shard.max_over_ranks(e2e_s)
+    e2e = {"value": w.pairs * world / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int(th.nbytes + yh.nbytes + 8 * (w.n_obj + 1)),
+           "d2h_bytes_per_step": int(oi.nbytes + op.nbytes),
+           "api": "lsgb_periodogram_host (C ABI), pinned host buffers, best period per object"}
+    if not np.array_equal(oi, best_idx.astype(np.uint32)):
+        e2e["mismatch_vs_device_path"] = True
+
     if rank != 0:
         return
     clocks = clk.summary()
@@ -447,7 +476,7 @@ def main():
                              ti[:, 0].cpu().numpy(), best_idx.astype(np.int32)))}
 
     # the other benchmark workloads (single object, generalized batch, long object)
-    if tensor_form and args.configs:
+    if tensor_form and args.configs and world == 1:
         extra["configs"] = {
             "single_3555obs_1e5freq_standard": measure_config(
                 eng, torch, dev, stream, flush, synth.single_object(), 0, 100_000),
@@ -458,7 +487,7 @@ def main():
         }
 
     # plain FP64 drop-in form on the first plain_freqs frequencies
-    if args.plain_freqs:
+    if args.plain_freqs and world == 1:
         wp = w.subset_freqs(args.plain_freqs)
         eng.run_device(0, "plain", t, y, None, wp.offsets, wp.fmin, wp.df, wp.n_freq, True, None,
                        bi, bp, stream)
@@ -478,29 +507,7 @@ def main():
                                "sample": f"first {args.plain_freqs} frequencies of the same grid"}
         extra["mixed_over_plain"] = value / pv
 
-    # e2e through the host-buffer C ABI with pinned inputs
-    th = torch.from_numpy(w.t).pin_memory().numpy()
-    yh = torch.from_numpy(w.y).pin_memory().numpy()
-    oi = torch.empty(w.n_obj, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
-    op = torch.empty(w.n_obj, dtype=torch.float64).pin_memory().numpy()
-    offs = np.ascontiguousarray(w.offsets, np.uint64)  # the caller's row offsets, once
-    for _ in range(2):
-        eng.run_host(0, "mixed", th, yh, None, offs, w.fmin, w.df, w.n_freq, True,
-                     out_idx=oi, out_power=op)
-    e2e_t = []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        eng.run_host(0, "mixed", th, yh, None, offs, w.fmin, w.df, w.n_freq, True,
-                     out_idx=oi, out_power=op)
-        e2e_t.append(time.perf_counter() - t0)
-    e2e = {"value": w.pairs / float(np.mean(e2e_t)), "unit": UNIT,
-           "h2d_bytes_per_step": int(th.nbytes + yh.nbytes + 8 * (w.n_obj + 1)),
-           "d2h_bytes_per_step": int(oi.nbytes + op.nbytes),
-           "api": "lsgb_periodogram_host (C ABI), pinned host buffers, best period per object"}
-    if not np.array_equal(oi, best_idx.astype(np.uint32)):
-        e2e["mismatch_vs_device_path"] = True
-
-    if not args.no_dropin:
+    if not args.no_dropin and world == 1:
         from gpu_lomb_scargle_gb300 import lombscarglegpu as lsg
         lib = lsg._library(False, "float")
         t32 = np.ascontiguousarray(w.t, np.float32)
@@ -532,7 +539,7 @@ def main():
                                "api": "LombScarglePy, libpylsnoerrorfloat.so, MODE 1, full pgram"}
         del pg
 
-    if args.serve_objects:
+    if args.serve_objects and world == 1:
         from gpu_lomb_scargle_gb300 import serve
         plan.close()
         eng.close()
@@ -552,7 +559,9 @@ def main():
                             "round(LogNormal(ln 80, 0.8)) in [10, 1000], 1e5 frequencies")
         extra["serving_loaded"] = rep2
 
-    cpu = cpu_baseline(w, args.cpu_freqs) if args.cpu_freqs else None
+    # the CPU baseline, and the side legs above, at one GPU only (under torchrun the other
+    # GPUs would wait on them)
+    cpu = cpu_baseline(w, args.cpu_freqs) if args.cpu_freqs and world == 1 else None
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None,
