@@ -89,3 +89,26 @@ def test_sliced_units_top3(eng, variant):
         gidx, gpw = pyoracle.top3(got[o])
         np.testing.assert_array_equal(r.best_idx[o], gidx)
         np.testing.assert_array_equal(r.best_power[o], gpw)
+
+
+@pytest.mark.parametrize("n_freq", [1, 2, 7])
+def test_sliced_units_with_few_frequencies(eng, n_freq):
+    """One long object at 1, 2 and 7 frequencies: a single tile cut into many slices, the
+    finishing pass covering only the first frequencies of its tile, and (at 1 and 2
+    frequencies) a top three padded with (0, 0)."""
+    w = synth.long_object(seed=7300, n_obs=5000, n_freq=n_freq)
+    offs = np.asarray(w.offsets, np.uint64)
+    ref = eng.run_host(0, "plain", w.t, w.y, None, offs, w.fmin, w.df, n_freq,
+                       normalize=True, want_pgram=True).pgram.reshape(1, n_freq)
+    r = eng.run_host(0, "mixed", w.t, w.y, None, offs, w.fmin, w.df, n_freq, normalize=True,
+                     want_pgram=True)
+    _, units = eng.launch_info()
+    assert units > 1  # 5,000 observations = 313 K-blocks: sliced
+    got = r.pgram.reshape(1, n_freq)
+    assert mixed_abs_err(got, ref) < MIXED_ATOL
+    assert not check_best(r.best_idx, ref, tol=MIXED_ATOL)
+    t3 = eng.run_host_top3(0, "mixed", w.t, w.y, None, offs, w.fmin, w.df, n_freq,
+                           normalize=True, want_pgram=True)
+    gidx, gpw = pyoracle.top3(t3.pgram.reshape(-1))
+    np.testing.assert_array_equal(t3.best_idx[0], gidx)
+    np.testing.assert_array_equal(t3.best_power[0], gpw)
